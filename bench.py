@@ -1,0 +1,333 @@
+"""Throughput of the q-SFT hot path on GB300: batched FP32 transforms vs plain FP64.
+
+Workload (the noisy robust configuration): q=4, n=20, b=7 (16384 bins), C=3
+random M_c, NSO delays with num_repeat=2 (P=21, 126 GWHT rows), S=1000 support
+vectors uniform in Z_4^20, |a|~U[1,10] with uniform phase, complex bin-domain
+AWGN at 10 dB SNR.  Synthetic, seeded inputs drawn with the reference's own
+generators on the host.
+
+A step = one batch of `--batch` transforms end to end: coset evaluation,
+GWHT, noise, peeling (all 15 loop iterations issued; finished jobs no-op) and
+result collection.  Every batch holds > 129 MB of bins, so successive steps
+stream from HBM rather than L2.
+
+  value  transforms/s with inputs resident on the device (CUDA events)
+  e2e    transforms/s through qsft_gb300.serve.transform_batch with host
+         inputs, host->device copies of those inputs and the device->host read
+         of every result inside the timed region (wall clock + sync)
+
+--impl reference times the reference's CPU algorithm (the numpy restatement in
+oracle/) on the host cores on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = dict(q=4, n=20, b=7, S=1000, C=3, R=2, snr_db=10.0, chan="nso", src="identity")
+METRIC = "sparse transforms/s (q=4,n=20,b=7,C=3,NSO R=2,S=1000,10 dB), FP32-batched vs FP64-plain"
+UNIT = "transforms/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--batch", type=int, default=16)
+    p.add_argument("--precision", default="fp32")
+    p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def make_requests(J, seed):
+    from qsft_gb300.serve import random_request
+    np.random.seed(seed)
+    w = WORKLOAD
+    return [random_request(w["q"], w["n"], w["b"], w["S"], C=w["C"], R=w["R"], snr_db=w["snr_db"], chan=w["chan"],
+                           src=w["src"]) for _ in range(J)]
+
+
+# ------------------------------------------------------------------ clocks
+class Clocks:
+    def __init__(self, gpu_index):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={q}", "--format=csv,noheader",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1].split()[0]))
+                mx = float(r[2].split()[0])
+                for nm, v in zip(names, r[5:9]):
+                    if "Active" in v and "Not" not in v:
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                continue
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU baseline
+def cpu_baseline(sample_rows=2, seed=0):
+    """The oracle (numpy restatement of the reference) on this host's cores:
+    evaluation of `sample_rows` of the 126 coset rows (threaded over all
+    cores, scaled to 126), plus the full GWHT of all rows and the full peeling
+    loop.  Returns (transforms/s, cores, sample description)."""
+    import oracle as O
+    w = WORKLOAD
+    q, n, b, S, C, R = w["q"], w["n"], w["b"], w["S"], w["C"], w["R"]
+    cores = os.cpu_count() or 1
+    np.random.seed(seed)
+    qa = dict(query_method="complex", num_subsample=C, b=b, delays_method_source="identity",
+              delays_method_channel="nso", num_repeat=R)
+    nsd = O.noise_sd_for_snr(S, w["snr_db"])
+    sig = O.OracleSignal(n, q, S, 1, 10, nsd, qa, skip_sampling=True)
+    P = n + 1
+    rows = C * R * P
+    # 1. evaluation sample
+    t0 = time.perf_counter()
+    for r in range(sample_rows):
+        c, rr = divmod(r, R * P)
+        X = O.coset_points(sig.Ms[c], sig.Ds[c][rr // P][rr % P], q).T
+        O.eval_points(X, sig.locq, sig.strengths, q, threads=cores)
+    t_eval = (time.perf_counter() - t0) * rows / sample_rows
+    # 2. GWHT of every row (bins from the closed form stand in for the samples' transform input)
+    Dst = [np.vstack(d) for d in sig.Ds]
+    U = O.closed_form_bins(sig.Ms, Dst, sig.locq, sig.strengths, q)
+    t0 = time.perf_counter()
+    for c in range(C):
+        for r in range(R * P):
+            O.gwht(U[c, r], q, b)
+    t_gwht = time.perf_counter() - t0
+    # 3. noise + peeling on the full bins
+    sig.Us = [[U[c, r * P:(r + 1) * P] for r in range(R)] for c in range(C)]
+    t0 = time.perf_counter()
+    O.OracleQSFT(num_subsample=C, num_repeat=R, b=b, reconstruct_method_source="identity",
+                 reconstruct_method_channel="nso").transform(sig)
+    t_peel = time.perf_counter() - t0
+    total = t_eval + t_gwht + t_peel
+    sample = (f"eval of {sample_rows}/{rows} coset rows (x{rows // sample_rows} scaled, {cores} threads) + "
+              f"full GWHT ({t_gwht:.2f}s) + full noise+peeling ({t_peel:.2f}s); est. {total:.1f}s/transform")
+    return 1.0 / total, cores, sample
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    for _ in range(max(args.warmup, 0) and 1):
+        pass
+    vals = []
+    info = None
+    for i in range(max(args.steps, 1)):
+        v, cores, sample = cpu_baseline(sample_rows=2, seed=args.seed + i)
+        vals.append(v)
+        info = (cores, sample)
+    value = float(np.mean(vals))
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+        "config": {"workload": "q4_n20_b7_C3_nso_R2_S1000_10dB", **WORKLOAD, "batch": 1,
+                   "parallelism": "cpu host threads"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": info[0], "kind": "port", "sample": info[1]},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+# ------------------------------------------------------------------ GPU
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+    from qsft_gb300 import _lib
+    from qsft_gb300.engine import Batch
+    from qsft_gb300.serve import transform_batch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+    lib = _lib.load()
+    J = args.batch
+    reqs = make_requests(J, args.seed + 1000 * rank)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(x):
+        if world == 1:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- device-resident throughput (value) + per-kernel timing
+    batch = Batch([r.spec() for r in reqs], precision=args.precision, device=dev)
+    stream = torch.cuda.current_stream()
+    ev = {k: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for k in ("eval", "gwht", "noise", "peel", "collect")}
+    acc = {k: 0.0 for k in ev}
+
+    def step(timed):
+        for k, fn in (("eval", batch.eval), ("gwht", batch.gwht), ("noise", batch.add_noise),
+                      ("peel", batch.peel), ("collect", batch.collect_async)):
+            if timed:
+                ev[k][0].record(stream)
+            fn()
+            if timed:
+                ev[k][1].record(stream)
+        if timed:
+            torch.cuda.synchronize()
+            for k in ev:
+                acc[k] += ev[k][0].elapsed_time(ev[k][1])
+
+    for _ in range(max(args.warmup, 3)):
+        step(False)
+    barrier()
+    clk = Clocks(local)
+    l0 = lib.qsft_launch_count()
+    t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0e.record(stream)
+    for _ in range(args.steps):
+        step(False)
+    t1e.record(stream)
+    barrier()
+    launches = (lib.qsft_launch_count() - l0)
+    dev_ms = t0e.elapsed_time(t1e)
+    clocks = clk.stop()
+    dev_ms = max_over_ranks(dev_ms)
+    value = J * args.steps * world / (dev_ms / 1e3)
+    # per-phase timing pass (separate, so the headline loop has no extra syncs)
+    for _ in range(args.steps):
+        step(True)
+    phase_ms = {k: v / args.steps for k, v in acc.items()}
+    res = batch.results()
+    truth = [set(map(tuple, r.locq.T.tolist())) for r in reqs]
+    found = [len(set(map(tuple, k.tolist())) & t) for (k, _, _, _), t in zip(res, truth)]
+    iters = [int(c.iter) for (_, _, _, c) in res]
+
+    # ---- end to end through the public API, host buffers
+    lat = []
+    h2d = d2h = 0
+    for i in range(max(args.warmup, 3) + args.steps):
+        barrier()
+        t = time.perf_counter()
+        out, b2 = transform_batch(reqs, precision=args.precision, return_batch=True)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t
+        if i >= max(args.warmup, 3):
+            lat.append(dt)
+    h2d = int(b2.i8.numel() + b2.A.numel() * b2.A.element_size() + b2.jobs_dev.numel() + 8 * b2.eval_prefix.numel()
+              + 8 * b2.bin_prefix.numel() + 4 * b2.gf.numel() + sum(8 * g.numel() for g in b2.gwht_groups.values()))
+    total_rows = sum(len(d) for d in out)
+    d2h = int(8 + 16 * J + b2.ctrl.numel() + total_rows * (b2.kstride + 16 + 4))
+    e2e_s = max_over_ranks(float(np.sum(lat)))
+    e2e = J * len(lat) * world / e2e_s
+
+    # ---- FP64 plain: one transform per launch sequence, FP64 everywhere
+    b64 = Batch([reqs[0].spec()], precision="fp64", device=dev)
+
+    def step64():
+        b64.eval(); b64.gwht(); b64.add_noise(); b64.peel(); b64.collect_async()
+    for _ in range(2):
+        step64()
+    barrier()
+    a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n64 = max(2, args.steps // 2)
+    a.record(stream)
+    for _ in range(n64):
+        step64()
+    z.record(stream)
+    torch.cuda.synchronize()
+    fp64_tps = n64 / (a.elapsed_time(z) / 1e3)
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+    # ---- roofline of the dominant kernel (coset evaluation) and of the GWHT
+    w = WORKLOAD
+    samples = w["C"] * w["R"] * (w["n"] + 1) * w["q"] ** w["b"]
+    npad = ((w["n"] + 15) // 16) * 16
+    eval_flops = 2.0 * samples * w["S"] * npad * J
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    bf16 = peaks.get("bf16_tflops", 1900.0)
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    e_ms = phase_ms["eval"]
+    g_ms = phase_ms["gwht"]
+    gwht_bytes = 2.0 * samples * 8 * J
+    roofline = {"kernel": "eval_cosets", "bound": "tensor", "achieved": eval_flops / (e_ms / 1e3) / 1e12,
+                "peak": bf16, "unit": "TFLOP/s", "traffic": None,
+                "peak_source": "measured" if "bf16_tflops" in peaks else "fallback"}
+    roofline["frac"] = roofline["achieved"] / roofline["peak"]
+    roof_gwht = {"kernel": "gwht", "bound": "hbm", "achieved": gwht_bytes / (g_ms / 1e3) / 1e9, "peak": hbm,
+                 "unit": "GB/s", "traffic": None, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
+    roof_gwht["frac"] = roof_gwht["achieved"] / roof_gwht["peak"]
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
+        "data": "synthetic (seeded, reference generators)",
+        "config": {"workload": "q4_n20_b7_C3_nso_R2_S1000_10dB", **WORKLOAD, "batch": J,
+                   "parallelism": f"replicas x{world}", "l2": "inputs > L2 (bins %.0f MB/step)" %
+                   (samples * 8 * J / 1e6)},
+        "latency_ms": {"p50": float(np.percentile(lat, 50) * 1e3), "p99": float(np.percentile(lat, 99) * 1e3),
+                       "note": "batch completion latency through transform_batch"},
+        "phase_ms": phase_ms,
+        "fp64_plain": {"value": fp64_tps, "unit": UNIT, "batched_fp32_over_fp64_plain": value / fp64_tps},
+        "accuracy": {"true_support_found": f"{sum(found)}/{J * w['S']}", "iterations": iters[:8]},
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "roofline": roofline, "roofline_gwht": roof_gwht, "clocks": clocks,
+    }
+    if not args.no_cpu_baseline:
+        v, cores, sample = cpu_baseline(sample_rows=2, seed=args.seed)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

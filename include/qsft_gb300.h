@@ -1,0 +1,245 @@
+/*
+ * qsft_gb300.h -- C ABI of the GB300 (sm_103a) q-SFT hot path.
+ *
+ * The reference (basics-lab/qsft) is a Python package whose hot path is:
+ *   coset query generation + function evaluation  (SubsampledSignal._subsample_qsft,
+ *       qsft/input_signal_subsampled.py:107-155,183-206; SyntheticSubsampledSignal
+ *       .subsample / sampling_function, synt_exp/synt_src/synthetic_signal.py:100-118)
+ *   q^b-point GWHT per (group, delay)              (qsft/utils.py:31-36; :264-266)
+ *   bin-domain AWGN                                (synthetic_signal.py:120-130)
+ *   singleton detection + peeling                  (qsft/qsft.py:151-255;
+ *       qsft/reconstruct.py:12-168; qsft/ReedSolomon.py:26-48)
+ * Each entry point below replaces one of those steps.  All entry points take
+ * plain device pointers and sizes (no framework types), run on the caller's
+ * CUDA stream, never synchronise, never allocate, and return a qsft_status.
+ * Every buffer is owned by the caller; qsft_workspace_layout() tells the
+ * caller how large the scratch regions must be.
+ *
+ * Batching: a call processes a batch of independent transform "jobs" that may
+ * have different shapes (q, n, b, C, R, P, S).  Jobs are described by an array
+ * of qsft_job records in device memory; packed operand arrays are addressed by
+ * the per-job offsets.  A batch of one job is the plain single-transform case.
+ */
+#ifndef QSFT_GB300_H
+#define QSFT_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef void* qsft_stream_t; /* a cudaStream_t (0 = legacy default stream) */
+
+typedef enum {
+  QSFT_OK = 0,
+  QSFT_ERR_ARG = -1,          /* bad shape / null pointer / unsupported parameter  */
+  QSFT_ERR_CUDA = -2,         /* a CUDA launch or runtime call failed               */
+  QSFT_ERR_TOO_LARGE = -3,    /* a shape exceeds a compiled limit (see QSFT_MAX_*)  */
+  QSFT_ERR_OVERFLOW = -4      /* a device table overflowed (reported via qsft_ctrl) */
+} qsft_status;
+
+/* compiled limits */
+#define QSFT_MAX_Q 32         /* alphabet size q (2..32)                              */
+#define QSFT_MAX_N 128        /* query length n                                       */
+#define QSFT_MAX_RS_T 16      /* Reed-Solomon correction radius t                     */
+#define QSFT_MAX_GF 4096      /* order q^s of the RS symbol field                      */
+
+/* qsft_eval_cosets works in tiles of this many samples of a job's C*R*P*B
+ * flattened samples; qsft_plan.eval_prefix counts these tiles               */
+#define QSFT_EVAL_TILE 1024
+
+/* precision of the complex data (float2 / double2 interleaved re,im) */
+#define QSFT_F32 4
+#define QSFT_F64 8
+
+/* channel / source decoding methods (QSFT reconstruct_method_channel / _source) */
+#define QSFT_CHAN_IDENTITY 0  /* noiseless [0;I] delays, qsft/reconstruct.py:12-31       */
+#define QSFT_CHAN_NSO 1       /* NSO soft decoding "nso1", qsft/reconstruct.py:100-113   */
+#define QSFT_SRC_IDENTITY 0
+#define QSFT_SRC_CODED 1      /* Reed-Solomon syndrome source code, reconstruct.py:34-51 */
+
+/*
+ * One transform.  Offsets are in ELEMENTS of the packed array they index.
+ *   M  (int8,  C x n x b, row-major per group)      -- Ms after get_MDU's permutation
+ *   D  (int8,  C x RP x n; RP = R*P, repeat-major)   -- np.vstack(Ds[c]) per group
+ *   K  (int8,  S x n)                                -- support k_s (synthetic signal)
+ *   A  (complex, S)                                  -- coefficients a_s
+ *   U  (complex, C x RP x B)                         -- samples, then bins
+ * The peeling workspace of a job starts at off_bin (bins), off_slot (hash
+ * slots) and off_ball (result balls) in the workspace arrays.
+ */
+typedef struct qsft_job {
+  int32_t q, n, b, C;
+  int32_t R, P, S, B;          /* B = q^b bins per row                              */
+  int32_t chan, src;           /* QSFT_CHAN_*, QSFT_SRC_*                           */
+  int32_t rs_s, rs_t;          /* RS: symbol field GF(q^s), radius t                */
+  int32_t rs_gf_off;           /* offset of this job's GF tables in gf_tables       */
+  int32_t max_iter;            /* peeling iteration cap (15 in the reference)       */
+  int32_t table_cap;           /* hash slots, power of two, >= 2*C*B                */
+  int32_t ball_cap;            /* capacity of the result ball store                 */
+  double cutoff;               /* energy threshold per bin entry (x RP)             */
+  int64_t peeling_max;         /* min(q^n, 2^62)                                    */
+  int64_t off_M, off_D, off_K, off_A, off_U;
+  int64_t off_bin, off_slot, off_ball;
+  uint64_t noise_seed;         /* device-noise key (qsft_add_noise_philox)          */
+  double noise_nu;             /* per-component noise sigma (0 = none)              */
+} qsft_job;
+
+/* per-job peeling state, device resident (zeroed by qsft_peel_init) */
+typedef struct qsft_ctrl {
+  int32_t done;                /* 1 once the reference's while-loop would exit      */
+  int32_t iter;                /* iterations run                                    */
+  int32_t n_single;            /* singletons found in the current iteration         */
+  int32_t n_multi;             /* multitons found in the current iteration          */
+  int32_t n_unique;            /* distinct balls peeled in the current iteration    */
+  int32_t n_balls;             /* distinct balls recorded so far (result size)      */
+  int32_t err;                 /* QSFT_ERR_OVERFLOW when a table filled up          */
+  int32_t pad;
+  int64_t num_peeling;         /* cumulative balls peeled                           */
+} qsft_ctrl;
+
+/*
+ * Everything a batched call needs.  All pointers are device pointers.  The
+ * struct itself lives in host memory and is passed by pointer.
+ */
+typedef struct qsft_plan {
+  int32_t njobs;
+  int32_t prec;                /* QSFT_F32 or QSFT_F64                              */
+  int32_t kstride;             /* bytes per decoded-k row in kbuf / ball_k (>= n)   */
+  int32_t flags;               /* QSFT_PLAN_* bits                                  */
+  int64_t total_bins;          /* sum of C*B over jobs                              */
+  int64_t total_slots;         /* sum of table_cap over jobs                        */
+  int64_t total_balls;         /* sum of ball_cap over jobs                         */
+  int64_t total_eval_tiles;    /* eval_prefix[njobs]                                */
+  int32_t max_q, max_n;        /* largest q and n over the jobs (launch sizing)     */
+  int32_t all_q_pow2;          /* 1 when every job's q is a power of two            */
+  int32_t max_rp;              /* largest R*P over the jobs                         */
+  const qsft_job* jobs;        /* [njobs]                                           */
+  const int64_t* eval_prefix;  /* [njobs+1] cumulative evaluation tiles             */
+  const int64_t* bin_prefix;   /* [njobs+1] cumulative C*B (== jobs[i].off_bin)     */
+  const int8_t* i8;            /* packed M, D, K                                    */
+  const void* A;               /* packed coefficients                               */
+  void* U;                     /* packed samples / bins                             */
+  const int32_t* gf_tables;    /* RS: exp | log | zech tables per field             */
+  const double* roots;         /* exp(2 pi i m / q) at ((q*32 + m)*2), q <= 32      */
+  /* peeling workspace (sizes from qsft_workspace_layout) */
+  uint8_t* kbuf;               /* [total_bins * kstride]   decoded k per bin        */
+  double* rho;                 /* [total_bins * 2]         FP64 coefficient per bin */
+  /* per-iteration dedupe table; entries are stamped with the iteration number
+   * in their high 32 bits so that no clearing is needed between iterations   */
+  int64_t* tab_key;            /* [total_slots]  (iter << 32) | (local bin + 1)     */
+  int64_t* tab_best;           /* [total_slots]  (iter << 32) | max local bin       */
+  int32_t* uniq;               /* [total_slots]  per-job list of occupied slots     */
+  int32_t* ball_tab;           /* [total_slots]  persistent k -> ball id + 1        */
+  uint8_t* ball_k;             /* [total_balls * kstride]                           */
+  double* ball_sum;            /* [total_balls * 2]                                 */
+  int32_t* ball_cnt;           /* [total_balls]                                     */
+  qsft_ctrl* ctrl;             /* [njobs]                                           */
+} qsft_plan;
+
+#define QSFT_PLAN_DETERMINISTIC 1  /* reserved */
+
+/* ---- library ---------------------------------------------------------- */
+int qsft_abi_version(void);                 /* returns 1 */
+const char* qsft_status_string(int status);
+/* device architecture the library was built for, e.g. 103 */
+int qsft_built_arch(void);
+/* number of kernels this library has launched in this process (all threads) */
+int64_t qsft_launch_count(void);
+
+/* ---- query generation + evaluation ------------------------------------- */
+/*
+ * Replaces SubsampledSignal._subsample_qsft's sampling of every coset
+ * (qsft/input_signal_subsampled.py:119-149) with the synthetic evaluation of
+ * SyntheticSubsampledSignal.sampling_function (synthetic_signal.py:100-102):
+ * U[c][r*P+p][l] = sum_s a_s * omega^(<(M_c l + d_{r,p}) mod q, k_s> mod q),
+ * omega = exp(2 pi i / q), l enumerated MSB-first (qsft/utils.py:107-108).
+ * Query points are never converted to decimal indices.
+ */
+int qsft_eval_cosets(const qsft_plan* plan, qsft_stream_t stream);
+
+/*
+ * Replaces SyntheticSubsampledSignal.subsample(query_indices)
+ * (synthetic_signal.py:108-118) for arbitrary query points given as q-ary
+ * digit rows X (npoints x n, int8, MSB-first like dec_to_qary_vec,
+ * qsft/utils.py:79-84).  out[i] = sum_s a_s omega^(<X_i, k_s> mod q).
+ */
+int qsft_eval_points(int prec, int q, int n, int S, const int8_t* X, int64_t npoints,
+                     const int8_t* K, const void* A, void* out, qsft_stream_t stream);
+
+/* ---- GWHT --------------------------------------------------------------- */
+/*
+ * Replaces gwht(x, q, b) = fftn(reshape(x,[q]*b)) / q^b (qsft/utils.py:31-36)
+ * as applied by _compute_subtransform (qsft/input_signal_subsampled.py:264-266),
+ * in place, on nrows rows of q^b complex values starting at data + row_off[i]
+ * (element offsets, device array).
+ */
+int qsft_gwht(int prec, int q, int b, void* data, const int64_t* row_off, int64_t nrows,
+              qsft_stream_t stream);
+
+/* ---- bin noise ---------------------------------------------------------- */
+/*
+ * Replaces the bin-domain AWGN of SyntheticSubsampledSignal.get_MDU
+ * (synthetic_signal.py:126-129): U += N(0, nu^2) + i N(0, nu^2) per entry,
+ * nu = jobs[j].noise_nu, drawn from a counter-based Philox-4x32-10 stream keyed
+ * by jobs[j].noise_seed (not numpy's stream: for reference-identical noise the
+ * host draws it and adds it with qsft_add_bins).
+ */
+int qsft_add_noise_philox(const qsft_plan* plan, qsft_stream_t stream);
+/* U[i] += X[i] for count complex values (host-drawn noise, uploaded) */
+int qsft_add_bins(int prec, void* U, const void* X, int64_t count, qsft_stream_t stream);
+
+/* ---- peeling ------------------------------------------------------------ */
+/* zero ctrl, the result ball store and its index (start of QSFT.transform) */
+int qsft_peel_init(const qsft_plan* plan, qsft_stream_t stream);
+/*
+ * One iteration of QSFT.transform's while-loop (qsft/qsft.py:151-241) for every
+ * job not yet done: detect zero/single/multi-tons in every bin of every group
+ * (qsft/qsft.py:162-193 with singleton_detection, qsft/reconstruct.py:132-168),
+ * record each singleton's coefficient (the `result` list, :209-217), dedupe
+ * singletons by k keeping the coefficient of the last (group, bin) in
+ * (i, j) order (`ball_values`, :216), subtract every ball from every group
+ * (:223-241), and apply the loop's stopping rules (:151, :204-205).
+ */
+int qsft_peel_iteration(const qsft_plan* plan, qsft_stream_t stream);
+/* max_iter iterations back to back (iterations of finished jobs are no-ops) */
+int qsft_peel_run(const qsft_plan* plan, int max_iter, qsft_stream_t stream);
+
+/*
+ * Gather the result of QSFT.transform for every job: the distinct k recorded
+ * by the peeling loop and the mean of their coefficients (the `gwht` dict,
+ * qsft/qsft.py:247-255).  Results of job j are written contiguously:
+ * out_index[2j] = first row, out_index[2j+1] = count; rows hold k in
+ * out_k[row*kstride ..] (n bytes used), the mean in out_val[2*row .. 2*row+1]
+ * and the number of singleton detections averaged in out_cnt[row].
+ * *out_total (device int64) must be zero on entry and receives the row count.
+ * Output capacity: plan->total_balls rows.
+ */
+int qsft_collect(const qsft_plan* plan, uint8_t* out_k, double* out_val, int32_t* out_cnt,
+                 int64_t* out_index, int64_t* out_total, qsft_stream_t stream);
+
+/* ---- Reed-Solomon syndrome decoding ------------------------------------- */
+/*
+ * Replaces ReedSolomon.syndrome_decode (qsft/ReedSolomon.py:26-48) for nrows
+ * syndromes at once: syms[row*2ts ..] holds the 2ts q-ary channel symbols of a
+ * row (2t GF(q^s) syndromes, MSB-first digits); k_out[row*n ..] receives the
+ * error values on the last n code positions (zero on a decoding failure).
+ * gf_tables: exp | log | zech tables of GF(q^s) (the layout qsft_job.rs_gf_off
+ * points at).
+ */
+int qsft_rs_decode(int q, int s, int t, int n, const int32_t* gf_tables, const uint8_t* syms,
+                   int64_t nrows, uint8_t* k_out, qsft_stream_t stream);
+
+/*
+ * Scratch sizes for a batch: given the jobs' (q, n, b, C, B) on the host,
+ * writes the counts of bins, hash slots, balls and the kstride, and fills the
+ * per-job offsets off_bin / off_slot / off_ball, table_cap and ball_cap.
+ */
+int qsft_workspace_layout(qsft_job* jobs_host, int njobs, int64_t* total_bins,
+                          int64_t* total_slots, int64_t* total_balls, int32_t* kstride);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QSFT_GB300_H */

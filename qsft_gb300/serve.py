@@ -1,0 +1,84 @@
+"""Batched transform API: many q-SFT requests per launch.
+
+``TransformRequest`` describes one synthetic-signal transform entirely on the
+host (support, coefficients, query matrices, noise level); ``transform_batch``
+packs any number of requests -- of any mix of shapes -- into one
+:class:`~qsft_gb300.engine.Batch`, runs evaluation, GWHT, device noise and
+peeling as one launch per phase, and returns one ``{k: coefficient}`` dict per
+request.  This is the call the serving loop and the benchmark make.
+"""
+import numpy as np
+
+from .engine import MAX_ITER, Batch, JobSpec
+from .query import get_Ms_and_Ds
+from .reed_solomon import ReedSolomon
+from .synthetic_signal import generate_signal_w
+
+
+class TransformRequest:
+    """One transform: f = sum_s a_s omega^<k_s, x>, sampled on C groups x R repeats
+    of P delays, plus bin-domain AWGN of standard deviation noise_sd (per-entry
+    nu = noise_sd / sqrt(2 q^b), synthetic_signal.py:126-129)."""
+
+    def __init__(self, q, n, b, locq, strengths, Ms, Ds, noise_sd=0.0, chan="nso", src="identity", t=None,
+                 noise_seed=0, cutoff=None, max_iter=MAX_ITER):
+        self.q, self.n, self.b = int(q), int(n), int(b)
+        self.locq = np.asarray(locq)                 # n x S (reference layout)
+        self.strengths = np.asarray(strengths)
+        self.Ms = [np.asarray(M) for M in Ms]        # C of n x b
+        self.Ds = [[np.asarray(d) for d in Dg] for Dg in Ds]   # C of R of P x n
+        self.noise_sd = float(noise_sd)
+        self.chan, self.src, self.t = chan, src, t
+        self.noise_seed = int(noise_seed)
+        self.cutoff = cutoff if cutoff is not None else 1e-9 + 1.5 * self.noise_sd ** 2 / self.q ** self.b
+        self.max_iter = max_iter
+
+    @property
+    def S(self):
+        return self.locq.shape[1]
+
+    def footprint_bytes(self, precision="fp32"):
+        """Device bytes this request occupies while in flight (bins + peeling scratch)."""
+        C, R, P, B = len(self.Ms), len(self.Ds[0]), self.Ds[0][0].shape[0], self.q ** self.b
+        es = 8 if precision == "fp32" else 16
+        bins = C * B
+        slots = 1 << int(np.ceil(np.log2(max(64, 2 * bins))))
+        kst = ((self.n + 15) // 16) * 16
+        return C * R * P * B * es + bins * (kst + 16) + slots * 24 + (bins + 64) * (kst + 20)
+
+    def spec(self):
+        C = len(self.Ms)
+        R, P = len(self.Ds[0]), self.Ds[0][0].shape[0]
+        D = np.stack([np.vstack(Dg) for Dg in self.Ds])
+        rs = ReedSolomon(self.n, self.t, self.q) if self.src == "coded" else None
+        return JobSpec(self.q, self.n, self.b, np.stack(self.Ms), D, R, P, chan=self.chan, src=self.src,
+                       cutoff=self.cutoff, K=self.locq.T, A=self.strengths, rs=rs, max_iter=self.max_iter,
+                       noise_nu=self.noise_sd / np.sqrt(2 * self.q ** self.b), noise_seed=self.noise_seed)
+
+
+def random_request(q, n, b, S, C=3, R=2, snr_db=None, chan="nso", src="identity", t=None, a_min=1.0, a_max=10.0,
+                   max_weight=None, noise_seed=None):
+    """A seeded synthetic request drawn with the reference's generators (host numpy RNG)."""
+    _, locq, strengths = generate_signal_w(n, q, S, a_min, a_max, full=False, max_weight=max_weight)
+    qa = dict(query_method="complex", num_subsample=C, b=b, delays_method_source=src, delays_method_channel=chan,
+              num_repeat=R, t=t)
+    Ms, Ds = get_Ms_and_Ds(n, q, **qa)
+    if snr_db is None or not np.isfinite(snr_db):
+        nsd = 0.0
+    else:
+        ea2 = (a_max ** 3 - a_min ** 3) / (3.0 * (a_max - a_min)) if a_max > a_min else a_min ** 2
+        nsd = float(np.sqrt(S * ea2 / (10.0 ** (snr_db / 10.0))))
+    seed = int(np.random.randint(0, 2 ** 62)) if noise_seed is None else noise_seed
+    return TransformRequest(q, n, b, locq, strengths, Ms, Ds, noise_sd=nsd, chan=chan, src=src, t=t, noise_seed=seed)
+
+
+def transform_batch(requests, precision="fp32", return_batch=False):
+    """Run every request in one packed batch; returns one dict k -> coefficient per request."""
+    batch = Batch([r.spec() for r in requests], precision=precision)
+    batch.eval()
+    batch.gwht()
+    batch.add_noise()
+    batch.peel(max(r.max_iter for r in requests))
+    out = [{tuple(int(x) for x in k): complex(v) for k, v in zip(keys, vals)}
+           for keys, vals, _, _ in batch.results()]
+    return (out, batch) if return_batch else out

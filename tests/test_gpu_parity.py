@@ -1,0 +1,212 @@
+"""Parity of the CUDA path (through the C ABI) with the oracle and with the
+reference's own outputs (golden fixtures).
+
+Tolerances: integer / index results (support sets, decoded k, bins chosen)
+must be identical.  Complex values: FP64 path relative error <= 1e-10;
+FP32 path relative error <= 2e-5 for samples / bins, and for recovered
+coefficients relative L2 <= 1e-5 against the reference's (noiseless and noisy
+alike, since the host draws the reference's noise), NMSE within 1% of the
+reference's NMSE.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from conftest import case_query_args, golden_cases, golden_dict, load_golden
+
+pytestmark = pytest.mark.gpu
+
+PRECS = ["fp64", "fp32"]
+REL = {"fp64": 1e-10, "fp32": 2e-5}
+
+
+def rel_err(a, b):
+    a, b = np.asarray(a), np.asarray(b)
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_gwht_matches_reference_pins(cuda, prec):
+    from qsft_gb300 import utils as U
+    z = load_golden("gwht_pins")
+    for key in z:
+        if key.startswith("x_"):
+            q, b = (int(t[1:]) for t in key[2:].split("_"))
+            assert rel_err(U.gwht(z[key], q, b, precision=prec), z["y" + key[1:]]) < REL[prec], key
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("q,b", [(2, 14), (3, 9), (4, 8), (5, 6), (7, 4), (20, 3), (20, 4), (16, 4), (32, 3)])
+def test_gwht_sizes_vs_oracle(cuda, prec, q, b):
+    """Single-pass and multi-pass (rows above the shared-memory budget) transforms."""
+    import torch
+    from qsft_gb300.engine import gwht_device
+    rs = np.random.RandomState(q * 100 + b)
+    x = rs.randn(3, q ** b) + 1j * rs.randn(3, q ** b)
+    t = torch.from_numpy(x).to(cuda).to(torch.complex128 if prec == "fp64" else torch.complex64)
+    got = gwht_device(t, q, b).cpu().numpy()
+    want = np.stack([O.gwht(r, q, b) for r in x])
+    assert rel_err(got, want) < REL[prec] * (3 if q == 20 else 1)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("q,n,S", [(4, 20, 1000), (20, 10, 37), (5, 100, 50), (3, 7, 1), (2, 128, 130)])
+def test_eval_points_vs_oracle(cuda, prec, q, n, S):
+    from qsft_gb300.engine import eval_points_device
+    rs = np.random.RandomState(n + S)
+    X = rs.randint(0, q, size=(3001, n))
+    K = rs.randint(0, q, size=(n, S))
+    A = rs.uniform(1, 10, S) * np.exp(1j * rs.uniform(0, 2 * np.pi, S))
+    got = eval_points_device(X, K.T, A, q, precision=prec).cpu().numpy()
+    want = O.eval_points(X, K, A, q)
+    assert rel_err(got, want) < (1e-11 if prec == "fp64" else 2e-6 * np.sqrt(S))
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("name", golden_cases(full_only=True))
+def test_sampling_and_gwht_vs_reference_bins(cuda, prec, name):
+    """eval_cosets + gwht of every coset against the reference's own bins."""
+    import qsft_gb300 as Q
+    z = load_golden(name)
+    q, n, S = int(z["q"]), int(z["n"]), int(z["S"])
+    np.random.seed(int(z["seed"]))
+    sig = Q.get_random_subsampled_signal(n=n, q=q, sparsity=S, a_min=1, a_max=10, noise_sd=float(z["noise_sd"]),
+                                         query_args=case_query_args(z), precision=prec)
+    got = sig._bins[int(z["b"])].cpu().numpy()
+    assert got.shape == z["Us_clean"].shape
+    assert rel_err(got, z["Us_clean"]) < REL[prec]
+
+
+def _run_product(z, prec, noise="host"):
+    import qsft_gb300 as Q
+    q, n, b, S, C, R = (int(z[k]) for k in "q n b S C R".split())
+    np.random.seed(int(z["seed"]))
+    sig = Q.get_random_subsampled_signal(n=n, q=q, sparsity=S, a_min=1, a_max=10, noise_sd=float(z["noise_sd"]),
+                                         query_args=case_query_args(z), precision=prec, noise=noise)
+    res = Q.QSFT(num_subsample=C, num_repeat=R, b=b, reconstruct_method_source=str(z["src"]),
+                 reconstruct_method_channel=str(z["ch"])).transform(sig, report=True, sort=True)
+    return sig, res
+
+
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("name", golden_cases())
+def test_transform_vs_reference(cuda, prec, name):
+    """QSFT.transform end to end against the reference run on the same seed."""
+    z = load_golden(name)
+    sig, res = _run_product(z, prec)
+    got, want = res["gwht"], golden_dict(z)
+    assert set(got) == set(want), f"support differs: +{len(set(got) - set(want))} -{len(set(want) - set(got))}"
+    l2 = np.sqrt(sum(abs(got[k] - want[k]) ** 2 for k in want) / sum(abs(v) ** 2 for v in want.values()))
+    assert l2 < (1e-10 if prec == "fp64" else 1e-5), l2
+    nm = O.nmse(sig.signal_w, got)
+    assert abs(nm - float(z["nmse"])) <= 0.01 * float(z["nmse"]) + 1e-12
+    assert res["n_samples"] == int(z["n_samples"])
+    assert np.array_equal(np.asarray(res["locations"]), np.asarray(z["locations"]))
+    assert res["max_hamming_weight"] == int(z["max_hamming_weight"])
+
+
+def test_rs_decode_vs_oracle(cuda):
+    from qsft_gb300 import ReedSolomon
+    from qsft_gb300.engine import rs_decode_batch
+    rng = np.random.RandomState(1)
+    for (n, t, q) in [(100, 8, 5), (20, 3, 3), (10, 2, 2), (30, 3, 7), (60, 5, 11)]:
+        rs = ReedSolomon(n, t, q)
+        ors = O.rs.ReedSolomonOracle(n, t, q)
+        D = rs.get_delay_matrix()
+        rows, want = [], []
+        for i in range(200):
+            if i % 2 == 0:   # valid weight <= t patterns
+                k = np.zeros(n, int)
+                w = rng.randint(0, t + 1)
+                k[rng.choice(n, w, replace=False)] = rng.randint(1, q, size=w)
+                syn = ((D @ k) % q)[1:]
+            else:            # arbitrary syndromes (multiton bins)
+                syn = rng.randint(0, q, size=2 * t * rs.s)
+            rows.append(syn)
+            dec = ors.syndrome_decode(list(syn))[0][0]
+            want.append(dec if dec.max(initial=0) < q else np.zeros(n, int))
+        got = rs_decode_batch(rs, np.array(rows))
+        assert np.array_equal(got, np.array(want)), (n, t, q)
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_coded_transform_vs_oracle(cuda, prec):
+    """RS-coded delays (parity vs the oracle: the reference needs galois)."""
+    import qsft_gb300 as Q
+    q, n, b, S, t, C, R = 5, 40, 3, 25, 4, 3, 2
+    qa = dict(query_method="complex", num_subsample=C, delays_method_source="coded", subsampling_method="qsft",
+              delays_method_channel="nso", num_repeat=R, b=b, t=t)
+    nsd = O.noise_sd_for_snr(S, 20)
+    np.random.seed(11)
+    sig = Q.get_random_subsampled_signal(n=n, q=q, sparsity=S, a_min=1, a_max=10, noise_sd=nsd, query_args=dict(qa),
+                                         max_weight=t, precision=prec)
+    res = Q.QSFT(num_subsample=C, num_repeat=R, b=b, reconstruct_method_source="coded",
+                 reconstruct_method_channel="nso", source_decoder=Q.get_reed_solomon_dec(n, t, q)).transform(sig)
+    np.random.seed(11)
+    osig = O.OracleSignal(n, q, S, 1, 10, nsd, dict(qa), max_weight=t)
+    ores = O.OracleQSFT(num_subsample=C, num_repeat=R, b=b, reconstruct_method_source="coded",
+                        reconstruct_method_channel="nso",
+                        source_decoder=O.rs.get_reed_solomon_dec(n, t, q)).transform(osig)
+    want = {tuple(int(x) for x in k): v for k, v in ores.items()}
+    assert set(res) == set(want)
+    l2 = np.sqrt(sum(abs(res[k] - want[k]) ** 2 for k in want) / sum(abs(v) ** 2 for v in want.values()))
+    assert l2 < (1e-10 if prec == "fp64" else 1e-5)
+    assert set(want) == set(osig.signal_w)
+
+
+def test_device_noise_statistics(cuda):
+    import torch
+    from qsft_gb300.engine import Batch, JobSpec
+    q, n, b, C, R, P = 4, 8, 6, 2, 2, 9
+    nu = 0.37
+    U = torch.zeros(C, R * P, q ** b, dtype=torch.complex64, device=cuda)
+    sp = JobSpec(q, n, b, np.zeros((C, n, b)), np.zeros((C, R * P, n)), R, P, U=U, noise_nu=nu, noise_seed=1234)
+    bt = Batch([sp], precision="fp32")
+    bt.add_noise()
+    x = bt.job_U(0).cpu().numpy().ravel()
+    for part in (x.real, x.imag):
+        assert abs(part.mean()) < 4 * nu / np.sqrt(part.size)
+        assert abs(part.std() / nu - 1) < 0.01
+    assert abs(np.corrcoef(x.real, x.imag)[0, 1]) < 0.01
+    bt2 = Batch([sp], precision="fp32")
+    bt2.add_noise()
+    assert np.array_equal(bt2.job_U(0).cpu().numpy().ravel(), x), "same seed must give the same noise"
+
+
+def test_batch_of_mixed_shapes_equals_single_runs(cuda):
+    """Jobs of different (q, n, b, C, R, P, S) in one packed batch give the
+    same results as each alone."""
+    from qsft_gb300.engine import Batch, JobSpec
+    rng = np.random.RandomState(5)
+    specs = []
+    for (q, n, b, S, R, ch) in [(4, 12, 5, 60, 2, "nso"), (3, 9, 4, 20, 1, "identity"), (20, 6, 2, 30, 3, "nso"),
+                                (2, 16, 8, 40, 2, "nso")]:
+        C = 3
+        locq = rng.randint(0, q, size=(S, n))
+        A = rng.uniform(1, 10, S) * np.exp(1j * rng.uniform(0, 2 * np.pi, S))
+        M = rng.randint(0, q, size=(C, n, b))
+        Dsrc = np.vstack((np.zeros(n), np.eye(n))).astype(int)
+        if ch == "nso":
+            offs = rng.randint(0, q, size=(R, n))
+            D1 = np.vstack([(o - Dsrc) % q for o in offs])
+        else:
+            D1 = Dsrc
+        D = np.stack([D1] * C)
+        nu = 0.05 if ch == "nso" else 0.0
+        cutoff = 1e-9 + 1.5 * 2 * nu ** 2      # qsft/qsft.py:125 with sigma^2 / q^b = 2 nu^2
+        specs.append(JobSpec(q, n, b, M, D, R, n + 1, chan=ch, K=locq, A=A, cutoff=cutoff,
+                             noise_nu=nu, noise_seed=99 + q))
+    outs = []
+    for sp in specs:
+        bt = Batch([sp], precision="fp32")
+        bt.eval(); bt.gwht(); bt.add_noise(); bt.peel()
+        outs.append(bt.results()[0])
+    bt = Batch(specs, precision="fp32")
+    bt.eval(); bt.gwht(); bt.add_noise(); bt.peel()
+    mixed = bt.results()
+    for (k1, v1, _, c1), (k2, v2, _, c2) in zip(outs, mixed):
+        d1 = {tuple(k): v for k, v in zip(k1, v1)}
+        d2 = {tuple(k): v for k, v in zip(k2, v2)}
+        assert set(d1) == set(d2) and len(d1) > 0
+        assert max(abs(d1[k] - d2[k]) for k in d1) < 1e-5
+        assert c1.iter == c2.iter
