@@ -250,10 +250,8 @@ def run_ours(args):
         dt = time.perf_counter() - t
         if i >= max(args.warmup, 3):
             lat.append(dt)
-    h2d = int(b2.i8.numel() + b2.A.numel() * b2.A.element_size() + b2.jobs_dev.numel() + 8 * b2.eval_prefix.numel()
-              + 8 * b2.bin_prefix.numel() + 4 * b2.gf.numel() + sum(8 * g.numel() for g in b2.gwht_groups.values()))
-    total_rows = sum(len(d) for d in out)
-    d2h = int(8 + 16 * J + b2.ctrl.numel() + total_rows * (b2.kstride + 16 + 4))
+    h2d = int(b2.h2d_bytes)
+    d2h = int(b2.d2h_bytes)
     e2e_s = max_over_ranks(float(np.sum(lat)))
     e2e = J * len(lat) * world / e2e_s
 

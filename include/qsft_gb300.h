@@ -36,7 +36,8 @@ typedef enum {
   QSFT_ERR_ARG = -1,          /* bad shape / null pointer / unsupported parameter  */
   QSFT_ERR_CUDA = -2,         /* a CUDA launch or runtime call failed               */
   QSFT_ERR_TOO_LARGE = -3,    /* a shape exceeds a compiled limit (see QSFT_MAX_*)  */
-  QSFT_ERR_OVERFLOW = -4      /* a device table overflowed (reported via qsft_ctrl) */
+  QSFT_ERR_OVERFLOW = -4,     /* a device table overflowed (reported via qsft_ctrl) */
+  QSFT_ERR_TIMEOUT = -5       /* a bounded device wait gave up (reported via status) */
 } qsft_status;
 
 /* compiled limits */
@@ -136,7 +137,19 @@ typedef struct qsft_plan {
   double* ball_sum;            /* [total_balls * 2]                                 */
   int32_t* ball_cnt;           /* [total_balls]                                     */
   qsft_ctrl* ctrl;             /* [njobs]                                           */
+  /* tensor-core evaluation (FP32 plans): work items are (job, support chunk of
+   * tc_smax entries, group of QSFT_TC_TILES tiles of 128 samples)              */
+  const int64_t* tc_prefix;    /* [njobs+1] cumulative work items, or NULL          */
+  int64_t total_tc_work;       /* tc_prefix[njobs]                                  */
+  int32_t tc_smax;             /* support entries per chunk                         */
+  int32_t tc_npad;             /* K extent: max n rounded up to 32, 64 or 128       */
+  int32_t min_q;               /* smallest q over the jobs                          */
+  int32_t tc_table_bytes;      /* max over jobs of C*b*q*tc_npad + C*R*P*tc_npad    */
+  int32_t* status;             /* [1] device word, 0 = ok, else a qsft_status       */
 } qsft_plan;
+
+/* tiles of 128 samples per tensor-core work item */
+#define QSFT_TC_TILES 16
 
 #define QSFT_PLAN_DETERMINISTIC 1  /* reserved */
 
@@ -158,6 +171,16 @@ int64_t qsft_launch_count(void);
  * Query points are never converted to decimal indices.
  */
 int qsft_eval_cosets(const qsft_plan* plan, qsft_stream_t stream);
+/*
+ * Same result as qsft_eval_cosets for FP32 plans, with the integer dot
+ * products <x, k_s> computed by the 5th-generation tensor cores
+ * (tcgen05.mma kind::f16: digits are exact in FP16 and the sums exact in the
+ * FP32 accumulator) into tensor memory; CUDA cores then reduce
+ * a_s * omega^(dot mod q).  Needs plan->tc_prefix / tc_smax / tc_npad, and U
+ * zeroed beforehand: partial sums (two column halves per sample, and one per
+ * support chunk) are added into U with vector reductions.
+ */
+int qsft_eval_cosets_tc(const qsft_plan* plan, qsft_stream_t stream);
 
 /*
  * Replaces SyntheticSubsampledSignal.subsample(query_indices)
@@ -213,7 +236,7 @@ int qsft_peel_run(const qsft_plan* plan, int max_iter, qsft_stream_t stream);
  * out_index[2j] = first row, out_index[2j+1] = count; rows hold k in
  * out_k[row*kstride ..] (n bytes used), the mean in out_val[2*row .. 2*row+1]
  * and the number of singleton detections averaged in out_cnt[row].
- * *out_total (device int64) must be zero on entry and receives the row count.
+ * *out_total (device int64) receives the row count (the call zeroes it first).
  * Output capacity: plan->total_balls rows.
  */
 int qsft_collect(const qsft_plan* plan, uint8_t* out_k, double* out_val, int32_t* out_cnt,

@@ -18,10 +18,14 @@ MAX_Q = 32
 MAX_N = 128
 MAX_RS_T = 16
 MAX_GF = 4096
+TC_TILES = 16     # QSFT_TC_TILES
+TC_TILE_M = 128
+TC_SUB_N = 128
 
 # exported symbols, in header order
 SYMBOLS = [
-    "qsft_abi_version", "qsft_status_string", "qsft_built_arch", "qsft_launch_count", "qsft_eval_cosets", "qsft_eval_points",
+    "qsft_abi_version", "qsft_status_string", "qsft_built_arch", "qsft_launch_count", "qsft_eval_cosets",
+    "qsft_eval_cosets_tc", "qsft_eval_points",
     "qsft_gwht", "qsft_add_noise_philox", "qsft_add_bins", "qsft_peel_init", "qsft_peel_iteration",
     "qsft_peel_run", "qsft_collect", "qsft_rs_decode", "qsft_workspace_layout",
 ]
@@ -71,6 +75,8 @@ class QsftPlan(ctypes.Structure):
         ("gf_tables", _P), ("roots", _P),
         ("kbuf", _P), ("rho", _P), ("tab_key", _P), ("tab_best", _P), ("uniq", _P), ("ball_tab", _P),
         ("ball_k", _P), ("ball_sum", _P), ("ball_cnt", _P), ("ctrl", _P),
+        ("tc_prefix", _P), ("total_tc_work", ctypes.c_int64), ("tc_smax", ctypes.c_int32),
+        ("tc_npad", ctypes.c_int32), ("min_q", ctypes.c_int32), ("tc_table_bytes", ctypes.c_int32), ("status", _P),
     ]
 
 
@@ -94,6 +100,7 @@ def load():
         "qsft_built_arch": ([], i32),
         "qsft_launch_count": ([], i64),
         "qsft_eval_cosets": ([plan_p, vp], i32),
+        "qsft_eval_cosets_tc": ([plan_p, vp], i32),
         "qsft_eval_points": ([i32, i32, i32, i32, vp, i64, vp, vp, vp, vp], i32),
         "qsft_gwht": ([i32, i32, i32, vp, vp, i64, vp], i32),
         "qsft_add_noise_philox": ([plan_p, vp], i32),

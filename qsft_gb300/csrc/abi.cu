@@ -146,6 +146,7 @@ extern "C" int qsft_collect(const qsft_plan* plan, uint8_t* out_k, double* out_v
   if (!plan || plan->njobs <= 0 || !plan->ctrl || !plan->ball_cnt || !plan->ball_k || !plan->ball_sum || !out_k ||
       !out_val || !out_cnt || !out_index || !out_total)
     return QSFT_ERR_ARG;
+  if (cudaMemsetAsync(out_total, 0, sizeof(int64_t), (cudaStream_t)stream) != cudaSuccess) return QSFT_ERR_CUDA;
   collect_kernel<<<plan->njobs, 256, 0, (cudaStream_t)stream>>>(*plan, out_k, out_val, out_cnt, out_index,
                                                                    reinterpret_cast<unsigned long long*>(out_total));
   QSFT_CUDA_CHECK_LAUNCH();

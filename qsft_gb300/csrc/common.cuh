@@ -1,5 +1,6 @@
 // Shared device helpers for the q-SFT kernels (sm_103a).
 #pragma once
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 

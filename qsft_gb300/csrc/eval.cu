@@ -45,10 +45,10 @@ __device__ __forceinline__ void stage_support(const int8_t* __restrict__ K, cons
   for (int idx = threadIdx.x; idx < EVAL_ST * q; idx += blockDim.x) {
     const int s = idx / q, r = idx - (idx / q) * q;
     c2<T> v = cmake<c2<T>>(0.0, 0.0);
-    if (s < cnt) {
-      const double2 a = to_d2(A[s0 + s]);
-      const double2 w = sW[r];
-      v = cmake<c2<T>>(a.x * w.x - a.y * w.y, a.x * w.y + a.y * w.x);
+    if (s < cnt) {  // product in T: GB300's FP64 rate is a small fraction of FP32
+      const c2<T> a = A[s0 + s];
+      const c2<T> w = cmake<c2<T>>(sW[r].x, sW[r].y);
+      v = cmul(a, w);
     }
     sT[idx] = v;
   }

@@ -18,6 +18,14 @@ from . import _lib
 from ._lib import QSFT_F32, QSFT_F64, QsftJob, QsftPlan, QsftCtrl, check, load, stream_handle
 
 EVAL_TILE = 1024  # QSFT_EVAL_TILE
+TC_TILE_M = 128   # samples per tensor-core tile
+TC_SUB_N = 128    # support entries per MMA sub-tile
+TC_SMEM_TARGET = 110 * 1024   # two CTAs per SM
+
+
+def tc_smem_bytes(npad, smax, max_q, table_bytes=0):
+    """Shared memory of the tensor-core evaluation kernel (mirrors eval_tc.cu)."""
+    return max(2048 + 128 * npad * 2 + smax * npad * 2 + smax * max_q * 8 + table_bytes, 80 * 1024)
 MAX_ITER = 15     # qsft/qsft.py:142
 
 _ROOTS = {}
@@ -85,34 +93,46 @@ class JobSpec:
             raise ValueError("coded source needs a ReedSolomon description")
 
 
+def layout_key(spec):
+    """Everything that fixes a job's place in the device workspace."""
+    rs = (spec.rs.s, spec.rs.t) if spec.rs is not None else None
+    return (spec.q, spec.n, spec.b, spec.C, spec.R, spec.P, spec.S, spec.chan, spec.src, rs)
+
+
 class Batch:
-    """Device-resident state of a batch of transforms (see module docstring)."""
+    """Device-resident state of a batch of transforms (see module docstring).
+
+    The workspace is allocated once per layout (the jobs' shapes); ``load``
+    replaces the inputs of a batch with the same layout through pinned host
+    staging buffers, so a serving loop re-uses one Batch per layout."""
 
     def __init__(self, specs, precision="fp32", device=None):
         self.lib = load()
-        self.specs = list(specs)
-        if not self.specs:
+        specs = list(specs)
+        if not specs:
             raise ValueError("empty batch")
         self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
         self.prec = precision_code(precision)
-        cdt = complex_dtype(self.prec)
-        J = len(self.specs)
+        self.cdt = complex_dtype(self.prec)
+        self.layout = tuple(layout_key(sp) for sp in specs)
+        self._build_layout(specs)
+        self._allocate()
+        self.load(specs)
+
+    # ------------------------------------------------------------ layout
+    def _build_layout(self, specs):
+        J = len(specs)
         jobs = (QsftJob * J)()
-        i8_parts, a_parts, gf_parts = [], [], []
         off_i8 = off_a = off_u = off_gf = 0
-        gf_index = {}
+        gf_index, gf_parts = {}, []
         eval_prefix = [0]
-        for j, sp in enumerate(self.specs):
+        for j, sp in enumerate(specs):
             jb = jobs[j]
             jb.q, jb.n, jb.b, jb.C = sp.q, sp.n, sp.b, sp.C
             jb.R, jb.P, jb.S, jb.B = sp.R, sp.P, sp.S, sp.B
             jb.chan = _lib.CHAN[sp.chan]
             jb.src = _lib.SRC[sp.src]
-            jb.max_iter = sp.max_iter
-            jb.cutoff = sp.cutoff
             jb.peeling_max = min(sp.q ** sp.n, 1 << 62)
-            jb.noise_nu = sp.noise_nu
-            jb.noise_seed = sp.noise_seed
             if sp.src == "coded":
                 key = (sp.q, sp.rs.s)
                 if key not in gf_index:
@@ -121,15 +141,14 @@ class Batch:
                     gf_parts.append(tb)
                     off_gf += tb.size
                 jb.rs_s, jb.rs_t, jb.rs_gf_off = sp.rs.s, sp.rs.t, gf_index[key]
-            for name, arr in (("off_M", sp.M), ("off_D", sp.D), ("off_K", sp.K)):
-                setattr(jb, name, off_i8)
-                if arr is not None:
-                    i8_parts.append(arr.astype(np.int8).ravel())
-                    off_i8 += arr.size
+            jb.off_M = off_i8
+            off_i8 += sp.M.size
+            jb.off_D = off_i8
+            off_i8 += sp.D.size
+            jb.off_K = off_i8
+            off_i8 += 0 if sp.K is None else sp.K.size
             jb.off_A = off_a
-            if sp.A is not None:
-                a_parts.append(sp.A)
-                off_a += sp.A.size
+            off_a += 0 if sp.A is None else sp.A.size
             jb.off_U = off_u
             off_u += sp.C * sp.R * sp.P * sp.B
             eval_prefix.append(eval_prefix[-1] + (sp.C * sp.R * sp.P * sp.B + EVAL_TILE - 1) // EVAL_TILE)
@@ -140,26 +159,53 @@ class Batch:
         self.total_bins, self.total_slots, self.total_balls = tb_.value, ts_.value, tl_.value
         self.kstride = ks_.value
         self.jobs_host = jobs
-        dev = self.device
+        self.n_i8, self.n_a, self.n_u = off_i8, off_a, off_u
+        self.eval_prefix_host = eval_prefix
+        self.gf_host = np.concatenate(gf_parts) if gf_parts else np.zeros(1, np.int32)
+        self.njobs = J
+        self.shapes = [(sp.q, sp.n, sp.b, sp.C, sp.R, sp.P, sp.S, sp.B) for sp in specs]
+        # tensor-core evaluation: K extent, support chunk, work items
+        maxn = max(sp.n for sp in specs)
+        self.tc_npad = 32 if maxn <= 32 else (64 if maxn <= 64 else 128)
+        maxq = max(sp.q for sp in specs)
+        self.tc_table_bytes = max(sp.C * (sp.b * sp.q + sp.R * sp.P) * self.tc_npad for sp in specs)
+        smax = TC_SUB_N
+        while tc_smem_bytes(self.tc_npad, smax + TC_SUB_N, maxq, self.tc_table_bytes) <= TC_SMEM_TARGET:
+            smax += TC_SUB_N
+        self.tc_smax = smax
+        # the tensor-core kernel needs its tables and one 128-entry support chunk in shared memory
+        self.tc_ok = tc_smem_bytes(self.tc_npad, smax, maxq, self.tc_table_bytes) <= 227 * 1024
+        tc_prefix = [0]
+        self.tc_needs_zero = False
+        for sp in specs:
+            tiles = -(-(sp.C * sp.R * sp.P * sp.B) // TC_TILE_M)
+            groups = -(-tiles // _lib.TC_TILES)
+            chunks = -(-sp.S // smax)
+            self.tc_needs_zero |= chunks != 1
+            tc_prefix.append(tc_prefix[-1] + chunks * groups)
+        self.tc_prefix_host = tc_prefix
+        rows = {}
+        for j, sp in enumerate(specs):
+            r = jobs[j].off_U + np.arange(sp.C * sp.R * sp.P, dtype=np.int64) * sp.B
+            rows.setdefault((sp.q, sp.b), []).append(r)
+        self.gwht_rows_host = {k: np.concatenate(v) for k, v in rows.items()}
+        self.max_iter = max(sp.max_iter for sp in specs)
 
-        def dt(a, dtype):
-            return torch.from_numpy(np.ascontiguousarray(a)).to(dev, dtype=dtype)
-
-        self.i8 = dt(np.concatenate(i8_parts) if i8_parts else np.zeros(1, np.int8), torch.int8)
-        a = np.concatenate(a_parts) if a_parts else np.zeros(1, np.complex128)
-        self.A = torch.from_numpy(a).to(dev).to(cdt)
-        self.U = torch.empty(max(off_u, 1), dtype=cdt, device=dev)
-        for j, sp in enumerate(self.specs):
-            if sp.U is not None:
-                n_el = sp.C * sp.R * sp.P * sp.B
-                self.U[jobs[j].off_U:jobs[j].off_U + n_el].copy_(sp.U.reshape(-1).to(cdt))
-        self.jobs_dev = torch.frombuffer(bytearray(bytes(jobs)), dtype=torch.uint8).to(dev)
-        self.eval_prefix = dt(np.array(eval_prefix, dtype=np.int64), torch.int64)
-        self.bin_prefix = dt(np.array([jobs[j].off_bin for j in range(J)] + [self.total_bins], dtype=np.int64),
-                             torch.int64)
-        self.gf = dt(np.concatenate(gf_parts) if gf_parts else np.zeros(1, np.int32), torch.int32)
-        self.roots = roots_table(dev)
+    def _allocate(self):
+        dev, J = self.device, self.njobs
         z = lambda n, d: torch.zeros(max(int(n), 1), dtype=d, device=dev)  # noqa: E731
+        self.i8 = z(self.n_i8, torch.int8)
+        self.A = z(self.n_a, self.cdt)
+        self.U = torch.empty(max(self.n_u, 1), dtype=self.cdt, device=dev)
+        self.jobs_dev = z(ctypes.sizeof(QsftJob) * J, torch.uint8)
+        up = lambda a, d: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dtype=d)  # noqa: E731
+        self.eval_prefix = up(np.array(self.eval_prefix_host, dtype=np.int64), torch.int64)
+        self.bin_prefix = up(np.array([self.jobs_host[j].off_bin for j in range(J)] + [self.total_bins],
+                                      dtype=np.int64), torch.int64)
+        self.tc_prefix = up(np.array(self.tc_prefix_host, dtype=np.int64), torch.int64)
+        self.gf = up(self.gf_host, torch.int32)
+        self.gwht_groups = {k: up(v, torch.int64) for k, v in self.gwht_rows_host.items()}
+        self.roots = roots_table(dev)
         self.kbuf = z(self.total_bins * self.kstride, torch.uint8)
         self.rho = z(self.total_bins * 2, torch.float64)
         self.tab_key = z(self.total_slots, torch.int64)
@@ -169,33 +215,74 @@ class Batch:
         self.ball_k = z(self.total_balls * self.kstride, torch.uint8)
         self.ball_sum = z(self.total_balls * 2, torch.float64)
         self.ball_cnt = z(self.total_balls, torch.int32)
-        self.ctrl = z(J * ctypes.sizeof(QsftCtrl), torch.uint8)
         self.out_k = z(self.total_balls * self.kstride, torch.uint8)
         self.out_val = z(self.total_balls * 2, torch.float64)
         self.out_cnt = z(self.total_balls, torch.int32)
-        self.out_index = z(2 * J, torch.int64)
-        self.out_total = z(1, torch.int64)
+        # metadata read back after a run, in one copy: total | index[2J] | ctrl[J] | status
+        cs = ctypes.sizeof(QsftCtrl) // 8
+        self.meta = z(1 + 2 * J + cs * J + 1, torch.int64)
+        self.out_total = self.meta[0:1]
+        self.out_index = self.meta[1:1 + 2 * J]
+        self.ctrl = self.meta[1 + 2 * J:1 + 2 * J + cs * J].view(torch.uint8)
+        self.status = self.meta[1 + 2 * J + cs * J:].view(torch.int32)
+        self.meta_host = torch.empty_like(self.meta, device="cpu").pin_memory()
+        # pinned staging for inputs
+        self.i8_host = torch.empty(self.i8.numel(), dtype=torch.int8).pin_memory()
+        self.A_host = torch.empty(self.A.numel(), dtype=self.cdt).pin_memory()
+        self.jobs_host_t = torch.empty(self.jobs_dev.numel(), dtype=torch.uint8).pin_memory()
         p = QsftPlan()
         p.njobs, p.prec, p.kstride, p.flags = J, self.prec, self.kstride, 0
         p.total_bins, p.total_slots, p.total_balls = self.total_bins, self.total_slots, self.total_balls
-        p.total_eval_tiles = eval_prefix[-1]
-        p.max_q = max(sp.q for sp in self.specs)
-        p.max_n = max(sp.n for sp in self.specs)
-        p.all_q_pow2 = int(all((sp.q & (sp.q - 1)) == 0 for sp in self.specs))
-        p.max_rp = max(sp.R * sp.P for sp in self.specs)
+        p.total_eval_tiles = self.eval_prefix_host[-1]
+        qs = [s[0] for s in self.shapes]
+        p.max_q, p.min_q = max(qs), min(qs)
+        p.max_n = max(s[1] for s in self.shapes)
+        p.all_q_pow2 = int(all((q & (q - 1)) == 0 for q in qs))
+        p.max_rp = max(s[4] * s[5] for s in self.shapes)
         ptr = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
         p.jobs, p.eval_prefix, p.bin_prefix = ptr(self.jobs_dev), ptr(self.eval_prefix), ptr(self.bin_prefix)
         p.i8, p.A, p.U, p.gf_tables, p.roots = ptr(self.i8), ptr(self.A), ptr(self.U), ptr(self.gf), ptr(self.roots)
         p.kbuf, p.rho, p.tab_key, p.tab_best = ptr(self.kbuf), ptr(self.rho), ptr(self.tab_key), ptr(self.tab_best)
         p.uniq, p.ball_tab, p.ball_k = ptr(self.uniq), ptr(self.ball_tab), ptr(self.ball_k)
         p.ball_sum, p.ball_cnt, p.ctrl = ptr(self.ball_sum), ptr(self.ball_cnt), ptr(self.ctrl)
+        p.tc_prefix, p.total_tc_work = ptr(self.tc_prefix), self.tc_prefix_host[-1]
+        p.tc_smax, p.tc_npad, p.tc_table_bytes = self.tc_smax, self.tc_npad, self.tc_table_bytes
+        p.status = ptr(self.status)
         self.plan = p
-        # rows per (q, b) size class for the GWHT
-        groups = {}
-        for j, sp in enumerate(self.specs):
-            rows = jobs[j].off_U + np.arange(sp.C * sp.R * sp.P, dtype=np.int64) * sp.B
-            groups.setdefault((sp.q, sp.b), []).append(rows)
-        self.gwht_groups = {k: dt(np.concatenate(v), torch.int64) for k, v in groups.items()}
+
+    # ------------------------------------------------------------ inputs
+    def load(self, specs, stream=None):
+        """Copy the inputs of `specs` (same layout as this batch) to the device."""
+        specs = list(specs)
+        if tuple(layout_key(sp) for sp in specs) != self.layout:
+            raise ValueError("specs do not match this batch's layout")
+        self.specs = specs
+        jobs = self.jobs_host
+        i8 = self.i8_host.numpy()
+        a = self.A_host.numpy()
+        for j, sp in enumerate(specs):
+            jb = jobs[j]
+            jb.max_iter = sp.max_iter
+            jb.cutoff = sp.cutoff
+            jb.noise_nu = sp.noise_nu
+            jb.noise_seed = sp.noise_seed
+            i8[jb.off_M:jb.off_M + sp.M.size] = sp.M.ravel()
+            i8[jb.off_D:jb.off_D + sp.D.size] = sp.D.ravel()
+            if sp.K is not None:
+                i8[jb.off_K:jb.off_K + sp.K.size] = sp.K.ravel()
+            if sp.A is not None:
+                a[jb.off_A:jb.off_A + sp.A.size] = sp.A
+        self.jobs_host_t.numpy()[:] = np.frombuffer(bytes(jobs), dtype=np.uint8)
+        st = stream if stream is not None else torch.cuda.current_stream(self.device)
+        with torch.cuda.stream(st):
+            self.i8.copy_(self.i8_host, non_blocking=True)
+            self.A.copy_(self.A_host, non_blocking=True)
+            self.jobs_dev.copy_(self.jobs_host_t, non_blocking=True)
+            for j, sp in enumerate(specs):
+                if sp.U is not None:
+                    n_el = sp.C * sp.R * sp.P * sp.B
+                    self.U[jobs[j].off_U:jobs[j].off_U + n_el].copy_(sp.U.reshape(-1).to(self.cdt))
+        self.h2d_bytes = self.i8.numel() + self.A.numel() * self.A.element_size() + self.jobs_dev.numel()
 
     # ------------------------------------------------------------ steps
     def job_U(self, j):
@@ -204,8 +291,14 @@ class Batch:
         n_el = sp.C * sp.R * sp.P * sp.B
         return self.U[jb.off_U:jb.off_U + n_el].view(sp.C, sp.R * sp.P, sp.B)
 
-    def eval(self, stream=None):
-        check(self.lib.qsft_eval_cosets(ctypes.byref(self.plan), stream_handle(stream)), "qsft_eval_cosets")
+    def eval(self, stream=None, tensor_cores=None):
+        """Coset evaluation; FP32 batches use the tensor-core kernel unless tensor_cores=False."""
+        use_tc = (self.prec == QSFT_F32 and self.tc_ok) if tensor_cores is None else bool(tensor_cores)
+        if use_tc:
+            self.U.zero_()   # the tensor-core kernel accumulates partial sums into U
+            check(self.lib.qsft_eval_cosets_tc(ctypes.byref(self.plan), stream_handle(stream)), "qsft_eval_cosets_tc")
+        else:
+            check(self.lib.qsft_eval_cosets(ctypes.byref(self.plan), stream_handle(stream)), "qsft_eval_cosets")
 
     def gwht(self, stream=None):
         for (q, b), rows in self.gwht_groups.items():
@@ -229,35 +322,54 @@ class Batch:
         check(self.lib.qsft_peel_run(ctypes.byref(self.plan), int(max_iter), sh), "qsft_peel_run")
 
     def collect_async(self, stream=None):
-        self.out_total.zero_()
         check(self.lib.qsft_collect(ctypes.byref(self.plan), ctypes.c_void_p(self.out_k.data_ptr()),
                                     ctypes.c_void_p(self.out_val.data_ptr()), ctypes.c_void_p(self.out_cnt.data_ptr()),
                                     ctypes.c_void_p(self.out_index.data_ptr()),
                                     ctypes.c_void_p(self.out_total.data_ptr()), stream_handle(stream)),
               "qsft_collect")
 
-    def ctrl_host(self):
-        raw = self.ctrl.cpu().numpy().tobytes()
-        return [QsftCtrl.from_buffer_copy(raw, j * ctypes.sizeof(QsftCtrl)) for j in range(len(self.specs))]
+    def ctrl_host(self, meta=None):
+        meta = self._read_meta() if meta is None else meta
+        J = self.njobs
+        raw = meta[1 + 2 * J:1 + 2 * J + (ctypes.sizeof(QsftCtrl) // 8) * J].tobytes()
+        return [QsftCtrl.from_buffer_copy(raw, j * ctypes.sizeof(QsftCtrl)) for j in range(J)]
 
-    def results(self):
-        """Per job: (keys (m, n) int64, values complex128 (m,), counts int32 (m,), ctrl)."""
-        self.collect_async()
-        total = int(self.out_total.item())
-        idx = self.out_index.cpu().numpy().reshape(-1, 2)
-        ks = self.out_k[:max(total, 1) * self.kstride].cpu().numpy().reshape(-1, self.kstride)
-        vals = self.out_val[:max(total, 1) * 2].cpu().numpy().reshape(-1, 2)
-        cnts = self.out_cnt[:max(total, 1)].cpu().numpy()
-        ctrls = self.ctrl_host()
+    def _read_meta(self):
+        self.meta_host.copy_(self.meta)   # synchronises with the stream
+        return self.meta_host.numpy()
+
+    def results(self, stream=None):
+        """Per job: (keys (m, n) int64, values complex128 (m,), counts int32 (m,), ctrl).
+
+        Two device->host copies: the metadata, then the used rows of the output."""
+        self.collect_async(stream)
+        meta = self._read_meta()
+        J = self.njobs
+        total = int(meta[0])
+        idx = meta[1:1 + 2 * J].reshape(-1, 2)
+        ctrls = self.ctrl_host(meta)
+        st = int(np.int64(meta[-1]).astype(np.int64) & 0xffffffff)
+        if st != 0:
+            st = st - (1 << 32) if st >= (1 << 31) else st
+            raise _lib.QsftError(f"device status {st}: {self.lib.qsft_status_string(st).decode()}")
+        rows = max(total, 1)
+        ks = self.out_k[:rows * self.kstride].cpu().numpy().reshape(-1, self.kstride)
+        vals = self.out_val[:rows * 2].cpu().numpy().reshape(-1, 2)
+        cnts = self.out_cnt[:rows].cpu().numpy()
+        self.d2h_bytes = self.meta.numel() * 8 + rows * (self.kstride + 16 + 4)
         out = []
-        for j, sp in enumerate(self.specs):
-            s, c = int(idx[j, 0]), int(idx[j, 1])
-            keys = ks[s:s + c, :sp.n].astype(np.int64)
-            v = vals[s:s + c, 0] + 1j * vals[s:s + c, 1]
+        for j, shape in enumerate(self.shapes):
             if ctrls[j].err:
                 raise _lib.QsftError(f"job {j}: device table overflow during peeling")
+            s, c = int(idx[j, 0]), int(idx[j, 1])
+            keys = ks[s:s + c, :shape[1]].astype(np.int64)
+            v = vals[s:s + c, 0] + 1j * vals[s:s + c, 1]
             out.append((keys, v, cnts[s:s + c].copy(), ctrls[j]))
         return out
+
+    def device_status(self):
+        """The kernels' status word (a bounded wait that gave up sets QSFT_ERR_TIMEOUT)."""
+        return int(self.status[0].item())
 
 
 def to_dict(keys, vals):

@@ -210,3 +210,44 @@ def test_batch_of_mixed_shapes_equals_single_runs(cuda):
         assert set(d1) == set(d2) and len(d1) > 0
         assert max(abs(d1[k] - d2[k]) for k in d1) < 1e-5
         assert c1.iter == c2.iter
+
+
+def _random_spec(rng, q, n, b, S, C, R, chan="nso"):
+    from qsft_gb300.engine import JobSpec
+    locq = rng.randint(0, q, size=(S, n))
+    A = rng.uniform(1, 10, S) * np.exp(1j * rng.uniform(0, 2 * np.pi, S))
+    M = rng.randint(0, q, size=(C, n, b))
+    Dsrc = np.vstack((np.zeros(n), np.eye(n))).astype(int)
+    offs = rng.randint(0, q, size=(R, n))
+    D1 = np.vstack([(o - Dsrc) % q for o in offs])
+    return JobSpec(q, n, b, M, np.stack([D1] * C), R, n + 1, chan=chan, K=locq, A=A, cutoff=1e-3)
+
+
+@pytest.mark.parametrize("shapes", [
+    [(4, 20, 7, 1000, 3, 2)],                      # the benchmark shape, q=4 fast path, K=32
+    [(2, 16, 9, 300, 3, 2)],                       # q=2 fast path
+    [(20, 10, 3, 37, 3, 3)],                       # runtime q, rows not a multiple of 128
+    [(3, 40, 5, 700, 2, 1)],                       # K=64
+    [(5, 100, 3, 50, 3, 1)],                       # K=128
+    [(20, 10, 3, 1500, 2, 1)],                     # support split over several chunks
+    [(4, 12, 5, 60, 3, 2), (3, 9, 4, 20, 3, 1), (20, 6, 2, 30, 3, 3), (2, 16, 8, 40, 3, 2)],  # mixed batch
+])
+def test_eval_tensor_cores_vs_cuda_cores_and_oracle(cuda, shapes):
+    """tcgen05 coset evaluation == CUDA-core evaluation == oracle (FP32 tolerance)."""
+    from qsft_gb300.engine import Batch
+    rng = np.random.RandomState(len(shapes) * 7 + shapes[0][0])
+    specs = [_random_spec(rng, *sh) for sh in shapes]
+    bt = Batch(specs, precision="fp32")
+    bt.eval(tensor_cores=True)
+    tc = [bt.job_U(j).cpu().numpy().copy() for j in range(len(specs))]
+    assert bt.device_status() == 0
+    bt.eval(tensor_cores=False)
+    cc = [bt.job_U(j).cpu().numpy().copy() for j in range(len(specs))]
+    for sp, a, c in zip(specs, tc, cc):
+        scale = np.abs(c).max()
+        assert np.max(np.abs(a - c)) / scale < 2e-6 * np.sqrt(sp.S)
+        # oracle on one coset row of each group
+        for g in range(sp.C):
+            X = O.coset_points(sp.M[g], sp.D[g][0], sp.q).T
+            want = O.eval_points(X, sp.K.T, sp.A, sp.q)
+            assert rel_err(a[g, 0], want) < 2e-6 * np.sqrt(sp.S)
