@@ -214,18 +214,18 @@ def run_ours(args):
             for k in ev:
                 acc[k] += ev[k][0].elapsed_time(ev[k][1])
 
+    batch.capture()                         # one CUDA graph per step
     for _ in range(max(args.warmup, 3)):
-        step(False)
+        batch.run()
     barrier()
     clk = Clocks(local)
-    l0 = lib.qsft_launch_count()
     t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0e.record(stream)
     for _ in range(args.steps):
-        step(False)
+        batch.run()
     t1e.record(stream)
     barrier()
-    launches = (lib.qsft_launch_count() - l0)
+    launches = batch.graph_launches * args.steps   # library kernels per replayed step
     dev_ms = t0e.elapsed_time(t1e)
     clocks = clk.stop()
     dev_ms = max_over_ranks(dev_ms)
@@ -234,7 +234,7 @@ def run_ours(args):
     for _ in range(args.steps):
         step(True)
     phase_ms = {k: v / args.steps for k, v in acc.items()}
-    res = batch.results()
+    res = batch.results(collected=True)
     truth = [set(map(tuple, r.locq.T.tolist())) for r in reqs]
     found = [len(set(map(tuple, k.tolist())) & t) for (k, _, _, _), t in zip(res, truth)]
     iters = [int(c.iter) for (_, _, _, c) in res]

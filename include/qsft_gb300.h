@@ -92,11 +92,12 @@ typedef struct qsft_ctrl {
   int32_t done;                /* 1 once the reference's while-loop would exit      */
   int32_t iter;                /* iterations run                                    */
   int32_t n_single;            /* singletons found in the current iteration         */
-  int32_t n_multi;             /* multitons found in the current iteration          */
+  int32_t n_multi;             /* multitons among all bins (kept up to date)        */
   int32_t n_unique;            /* distinct balls peeled in the current iteration    */
   int32_t n_balls;             /* distinct balls recorded so far (result size)      */
   int32_t err;                 /* QSFT_ERR_OVERFLOW when a table filled up          */
-  int32_t pad;
+  int32_t n_cand;              /* bins above the energy cutoff queued for decoding  */
+  int32_t n_dirty[2];          /* bins changed by the peel of an iteration (parity) */
   int64_t num_peeling;         /* cumulative balls peeled                           */
 } qsft_ctrl;
 
@@ -137,6 +138,12 @@ typedef struct qsft_plan {
   double* ball_sum;            /* [total_balls * 2]                                 */
   int32_t* ball_cnt;           /* [total_balls]                                     */
   qsft_ctrl* ctrl;             /* [njobs]                                           */
+  uint8_t* bin_status;         /* [total_bins] 0 zeroton, 1 multiton, 2 singleton  */
+  int32_t* bin_stamp;          /* [total_bins] last iteration that changed the bin  */
+  int32_t* dirty;              /* [2 * total_bins] changed bins, by iteration parity */
+  int32_t* cand;               /* [total_bins] bins queued for decoding             */
+  int32_t* done_count;         /* [1] jobs whose loop has ended (peel kernels exit
+                                * at once when it reaches njobs)                    */
   /* tensor-core evaluation (FP32 plans): work items are (job, support chunk of
    * tc_smax entries, group of QSFT_TC_TILES tiles of 128 samples)              */
   const int64_t* tc_prefix;    /* [njobs+1] cumulative work items, or NULL          */
@@ -145,6 +152,10 @@ typedef struct qsft_plan {
   int32_t tc_npad;             /* K extent: max n rounded up to 32, 64 or 128       */
   int32_t min_q;               /* smallest q over the jobs                          */
   int32_t tc_table_bytes;      /* max over jobs of C*b*q*tc_npad + C*R*P*tc_npad    */
+  int32_t tc_entry_bytes;      /* shared-memory table bytes per support entry:
+                                * q*q*4 when every job has the same q in {2, 4}
+                                * (pair table), else max_q*8                        */
+  int32_t pad2_;
   int32_t* status;             /* [1] device word, 0 = ok, else a qsft_status       */
 } qsft_plan;
 
@@ -218,14 +229,18 @@ int qsft_add_bins(int prec, void* U, const void* X, int64_t count, qsft_stream_t
 int qsft_peel_init(const qsft_plan* plan, qsft_stream_t stream);
 /*
  * One iteration of QSFT.transform's while-loop (qsft/qsft.py:151-241) for every
- * job not yet done: detect zero/single/multi-tons in every bin of every group
+ * job not yet done: classify every bin of every group as zero/single/multiton
  * (qsft/qsft.py:162-193 with singleton_detection, qsft/reconstruct.py:132-168),
  * record each singleton's coefficient (the `result` list, :209-217), dedupe
  * singletons by k keeping the coefficient of the last (group, bin) in
  * (i, j) order (`ball_values`, :216), subtract every ball from every group
  * (:223-241), and apply the loop's stopping rules (:151, :204-205).
+ * `first` = 1 for the first iteration after qsft_peel_init (every bin is
+ * classified); later iterations re-classify only the bins the previous
+ * iteration's subtractions changed -- the others keep their class, which is a
+ * function of the bin's unchanged values, so the outcome is the same.
  */
-int qsft_peel_iteration(const qsft_plan* plan, qsft_stream_t stream);
+int qsft_peel_iteration(const qsft_plan* plan, int first, qsft_stream_t stream);
 /* max_iter iterations back to back (iterations of finished jobs are no-ops) */
 int qsft_peel_run(const qsft_plan* plan, int max_iter, qsft_stream_t stream);
 

@@ -57,7 +57,8 @@ class QsftCtrl(ctypes.Structure):
     _fields_ = [
         ("done", ctypes.c_int32), ("iter", ctypes.c_int32), ("n_single", ctypes.c_int32),
         ("n_multi", ctypes.c_int32), ("n_unique", ctypes.c_int32), ("n_balls", ctypes.c_int32),
-        ("err", ctypes.c_int32), ("pad", ctypes.c_int32), ("num_peeling", ctypes.c_int64),
+        ("err", ctypes.c_int32), ("n_cand", ctypes.c_int32), ("n_dirty", ctypes.c_int32 * 2),
+        ("num_peeling", ctypes.c_int64),
     ]
 
 
@@ -75,8 +76,10 @@ class QsftPlan(ctypes.Structure):
         ("gf_tables", _P), ("roots", _P),
         ("kbuf", _P), ("rho", _P), ("tab_key", _P), ("tab_best", _P), ("uniq", _P), ("ball_tab", _P),
         ("ball_k", _P), ("ball_sum", _P), ("ball_cnt", _P), ("ctrl", _P),
+        ("bin_status", _P), ("bin_stamp", _P), ("dirty", _P), ("cand", _P), ("done_count", _P),
         ("tc_prefix", _P), ("total_tc_work", ctypes.c_int64), ("tc_smax", ctypes.c_int32),
-        ("tc_npad", ctypes.c_int32), ("min_q", ctypes.c_int32), ("tc_table_bytes", ctypes.c_int32), ("status", _P),
+        ("tc_npad", ctypes.c_int32), ("min_q", ctypes.c_int32), ("tc_table_bytes", ctypes.c_int32),
+        ("tc_entry_bytes", ctypes.c_int32), ("pad2_", ctypes.c_int32), ("status", _P),
     ]
 
 
@@ -106,7 +109,7 @@ def load():
         "qsft_add_noise_philox": ([plan_p, vp], i32),
         "qsft_add_bins": ([i32, vp, vp, i64, vp], i32),
         "qsft_peel_init": ([plan_p, vp], i32),
-        "qsft_peel_iteration": ([plan_p, vp], i32),
+        "qsft_peel_iteration": ([plan_p, i32, vp], i32),
         "qsft_peel_run": ([plan_p, i32, vp], i32),
         "qsft_collect": ([plan_p, vp, vp, vp, vp, vp, vp], i32),
         "qsft_rs_decode": ([i32, i32, i32, i32, vp, vp, i64, vp, vp], i32),

@@ -3,6 +3,7 @@
 #include <stdio.h>
 
 #include <atomic>
+#include <mutex>
 
 #include "common.cuh"
 #include "rs.cuh"
@@ -69,6 +70,30 @@ static int64_t next_pow2(int64_t v) {
 
 static std::atomic<long long> g_launches{0};
 void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+bool ensure_smem(const void* func, int bytes) {
+  struct Entry {
+    const void* f;
+    int dev;
+    int bytes;
+  };
+  static Entry table[256];
+  static int used = 0;
+  static std::mutex mu;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  std::lock_guard<std::mutex> lock(mu);
+  for (int i = 0; i < used; ++i)
+    if (table[i].f == func && table[i].dev == dev) {
+      if (table[i].bytes >= bytes) return true;
+      if (cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) return false;
+      table[i].bytes = bytes;
+      return true;
+    }
+  if (cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) return false;
+  if (used < 256) table[used++] = Entry{func, dev, bytes};
+  return true;
+}
 
 }  // namespace qsft
 

@@ -75,6 +75,10 @@ inline int ceil_div(int64_t a, int64_t b) { return (int)((a + b - 1) / b); }
 namespace qsft {
 // kernels launched by this library since load (qsft_launch_count)
 void count_launch();
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) only when a kernel needs more
+// than it was last given on this device: keeps launches free of non-stream API
+// calls after the first, so they can be captured into CUDA graphs
+bool ensure_smem(const void* func, int bytes);
 }  // namespace qsft
 
 #define QSFT_CUDA_CHECK_LAUNCH()                         \

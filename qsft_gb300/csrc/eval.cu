@@ -209,8 +209,7 @@ template <typename T, int NW, bool POW2>
 static int launch_cosets(const qsft_plan* plan, cudaStream_t st) {
   const size_t sm = EvalSmem<T, NW>::bytes(plan->max_q);
   auto kern = eval_cosets_kernel<T, NW, POW2>;
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
-    return QSFT_ERR_CUDA;
+  if (!ensure_smem((const void*)kern, (int)sm)) return QSFT_ERR_CUDA;
   if (plan->total_eval_tiles <= 0) return QSFT_OK;
   kern<<<(unsigned)plan->total_eval_tiles, EVAL_THREADS, sm, st>>>(*plan);
   QSFT_CUDA_CHECK_LAUNCH();
@@ -233,8 +232,7 @@ static int launch_points(int q, int n, int S, const int8_t* X, int64_t np, const
                          void* out, cudaStream_t st) {
   const size_t sm = EvalSmem<T, NW>::bytes(q);
   auto kern = eval_points_kernel<T, NW, POW2>;
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
-    return QSFT_ERR_CUDA;
+  if (!ensure_smem((const void*)kern, (int)sm)) return QSFT_ERR_CUDA;
   const int64_t grid = (np + EVAL_TILE - 1) / EVAL_TILE;
   kern<<<(unsigned)grid, EVAL_THREADS, sm, st>>>(q, n, S, X, np, K, reinterpret_cast<const c2<T>*>(A),
                                                  reinterpret_cast<c2<T>*>(out));

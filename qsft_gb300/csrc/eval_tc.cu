@@ -121,8 +121,8 @@ __device__ __forceinline__ uint32_t pack_h2(uint32_t lo, uint32_t hi) {
   return *reinterpret_cast<const uint32_t*>(&h);
 }
 
-inline size_t smem_bytes(int npad, int smax, int max_q, int64_t table_bytes) {
-  size_t b = HDR + (size_t)TILE_M * npad * 2 + (size_t)smax * npad * 2 + (size_t)smax * max_q * sizeof(float2) +
+inline size_t smem_bytes(int npad, int smax, int entry_bytes, int64_t table_bytes) {
+  size_t b = HDR + (size_t)TILE_M * npad * 2 + (size_t)smax * npad * 2 + (size_t)smax * entry_bytes +
              (size_t)table_bytes;
   return b < (size_t)MIN_SMEM ? (size_t)MIN_SMEM : b;
 }
@@ -151,29 +151,35 @@ __device__ __forceinline__ void red_add_v2(float* addr, float x, float y) {
 }
 
 // acc[0..3] += sum over 16 TMEM columns (support entries s_rel .. s_rel+15)
-// of table[s][dot mod q]; four independent accumulation chains.
+// of a_s omega^(dot mod q).
+//
+// q in {2, 4} (QT): the table holds one row per PAIR of support entries,
+// T[p][ma][mb] = a_2p omega^ma + a_2p+1 omega^mb (q*q entries of 8 bytes), so
+// one lookup serves two columns.  v + 2^23 puts the integer v in the FP32
+// mantissa, so fma(v, S, 2^23) holds S*v in its low bits; masking gives the
+// byte offset S*(v mod q) for S = 8*QT (column 2p) and S = 8 (column 2p+1).
+// The pair-row base is aligned to the table row size times 8, so OR adds the
+// offsets and the row offset of pair p rides in the load's immediate.
 template <int QT, int C>
-__device__ __forceinline__ void add_col(const uint32_t (&r)[16], uint32_t rowbase, uint64_t (&acc)[4]) {
-  // v + 2^23 puts the integer v (< 2^20) in the mantissa, so fma(v, 8, 2^23) &
-  // ((q-1) << 3) is 8 * (v mod q): the byte offset of the entry within the row
-  // of support s.  rowbase is 8*QT*16-aligned, so OR adds it, and the column's
-  // row offset C*8*QT (< 8*QT*16) rides in the load's immediate.
-  constexpr uint32_t mask8 = (uint32_t)(QT - 1) << 3;
-  const uint32_t off = (__float_as_uint(fmaf(__uint_as_float(r[C]), 8.0f, 8388608.0f)) & mask8) | rowbase;
-  acc[C & 3] = add_f32x2(acc[C & 3], lds64_imm<C * QT * 8>(off));
+__device__ __forceinline__ void add_pair(const uint32_t (&r)[16], uint32_t rowbase, uint64_t (&acc)[4]) {
+  constexpr uint32_t mask_a = (uint32_t)(QT - 1) * QT * 8, mask_b = (uint32_t)(QT - 1) * 8;
+  const uint32_t ba = __float_as_uint(fmaf(__uint_as_float(r[C]), (float)(QT * 8), 8388608.0f));
+  const uint32_t bb = __float_as_uint(fmaf(__uint_as_float(r[C + 1]), 8.0f, 8388608.0f));
+  const uint32_t off = (ba & mask_a) | ((bb & mask_b) | rowbase);
+  acc[(C >> 1) & 3] = add_f32x2(acc[(C >> 1) & 3], lds64_imm<(C >> 1) * QT * QT * 8>(off));
 }
 template <int QT, int C>
-__device__ __forceinline__ void add_cols(const uint32_t (&r)[16], uint32_t rowbase, uint64_t (&acc)[4]) {
+__device__ __forceinline__ void add_pairs(const uint32_t (&r)[16], uint32_t rowbase, uint64_t (&acc)[4]) {
   if constexpr (C < 16) {
-    add_col<QT, C>(r, rowbase, acc);
-    add_cols<QT, C + 1>(r, rowbase, acc);
+    add_pair<QT, C>(r, rowbase, acc);
+    add_pairs<QT, C + 2>(r, rowbase, acc);
   }
 }
 template <int QT>
 __device__ __forceinline__ void reduce16(const uint32_t (&r)[16], uint32_t sT_addr, const float2* __restrict__ sT,
                                          int s_rel, int q, ModQ mq, uint64_t (&acc)[4]) {
   if constexpr (QT == 2 || QT == 4) {
-    add_cols<QT, 0>(r, sT_addr + (uint32_t)s_rel * QT * 8, acc);
+    add_pairs<QT, 0>(r, sT_addr + (uint32_t)(s_rel >> 1) * QT * QT * 8, acc);
   } else {
     const float2* rowp = sT + (size_t)s_rel * q;
 #pragma unroll
@@ -220,7 +226,7 @@ __global__ void __launch_bounds__(THREADS, 2) eval_tc_kernel(qsft_plan plan) {
   float2* sT = reinterpret_cast<float2*>(sB + (size_t)smax * NPAD * 2);  // smax x q
   // digit tables: sX[(c*b + t)*q + v] = NPAD bytes (M[c][i][t] * v) mod q, i < n;
   //               sD[c*RP + rp]       = NPAD bytes d_{c,rp}[i]
-  unsigned char* sX = reinterpret_cast<unsigned char*>(sT + (size_t)smax * plan.max_q);
+  unsigned char* sX = reinterpret_cast<unsigned char*>(sT) + (size_t)smax * plan.tc_entry_bytes;
 
   constexpr uint32_t SBO = NPAD * 16;  // bytes between 8-row groups
   constexpr uint32_t IDESC = make_idesc(TILE_M, SUB_N);
@@ -279,15 +285,33 @@ __global__ void __launch_bounds__(THREADS, 2) eval_tc_kernel(qsft_plan plan) {
     uint4 v = make_uint4(pack_h2(d[0], d[1]), pack_h2(d[2], d[3]), pack_h2(d[4], d[5]), pack_h2(d[6], d[7]));
     *reinterpret_cast<uint4*>(sB + (r >> 3) * SBO + kc * 128 + (r & 7) * 16) = v;
   }
-  for (int idx = tid; idx < rows_b * q; idx += THREADS) {
-    const int s = idx / q, rr = idx - (idx / q) * q;
-    float2 v = make_float2(0.f, 0.f);
-    if (s < scnt) {  // FP32 product: GB300's FP64 rate is a small fraction of FP32
-      const float2 a = A[s];
-      const float2 wr = sW[rr];
-      v = make_float2(fmaf(a.x, wr.x, -a.y * wr.y), fmaf(a.x, wr.y, a.y * wr.x));
+  // FP32 products: GB300's FP64 rate is a small fraction of FP32
+  if constexpr (QT == 2 || QT == 4) {
+    for (int idx = tid; idx < (rows_b / 2) * QT * QT; idx += THREADS) {
+      const int p = idx / (QT * QT), ma = (idx / QT) % QT, mb = idx % QT;
+      float2 v = make_float2(0.f, 0.f);
+      if (2 * p < scnt) {
+        const float2 a = A[2 * p], w2 = sW[ma];
+        v = make_float2(fmaf(a.x, w2.x, -a.y * w2.y), fmaf(a.x, w2.y, a.y * w2.x));
+      }
+      if (2 * p + 1 < scnt) {
+        const float2 a = A[2 * p + 1], w2 = sW[mb];
+        v.x += fmaf(a.x, w2.x, -a.y * w2.y);
+        v.y += fmaf(a.x, w2.y, a.y * w2.x);
+      }
+      sT[idx] = v;
     }
-    sT[idx] = v;
+  } else {
+    for (int idx = tid; idx < rows_b * q; idx += THREADS) {
+      const int s = idx / q, rr = idx - (idx / q) * q;
+      float2 v = make_float2(0.f, 0.f);
+      if (s < scnt) {
+        const float2 a = A[s];
+        const float2 wr = sW[rr];
+        v = make_float2(fmaf(a.x, wr.x, -a.y * wr.y), fmaf(a.x, wr.y, a.y * wr.x));
+      }
+      sT[idx] = v;
+    }
   }
   const int C = job->C;
   unsigned char* sD = sX + (size_t)C * b * q * NPAD;
@@ -455,7 +479,9 @@ __global__ void __launch_bounds__(THREADS, 2) eval_tc_kernel(qsft_plan plan) {
 
 template <int NPAD, int QT>
 static int launch(const qsft_plan* p, cudaStream_t st) {
-  const size_t sm = smem_bytes(NPAD, p->tc_smax, p->max_q, p->tc_table_bytes);
+  const int pairs = (QT == 2 || QT == 4);
+  if (p->tc_entry_bytes != (pairs ? QT * QT * 4 : p->max_q * 8)) return QSFT_ERR_ARG;
+  const size_t sm = smem_bytes(NPAD, p->tc_smax, p->tc_entry_bytes, p->tc_table_bytes);
   if (sm > 227 * 1024) return QSFT_ERR_TOO_LARGE;
   auto kern = eval_tc_kernel<NPAD, QT>;
   if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)

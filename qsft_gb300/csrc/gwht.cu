@@ -8,6 +8,11 @@
 // elements), runs the radix-q DFT along each axis of the tile, and writes the
 // tile back.  When the whole row fits (q^b complex values within the shared
 // memory budget) one pass does everything and HBM sees one read and one write.
+// Rows above 48 KB whose q^k-way split fits 64 KB per part (k with q^k <= 8)
+// use a thread-block cluster per row instead (one HBM read and write, parts
+// exchanged through distributed shared memory).
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 
 namespace qsft {
@@ -138,6 +143,185 @@ __global__ void __launch_bounds__(512) gwht_pass_kernel(c2<T>* __restrict__ data
   }
 }
 
+// ---------------------------------------------------------------- cluster path
+// A row of B = q^b values is split over a cluster of CS = q^k CTAs (CTA j holds
+// elements [j*Bp, (j+1)*Bp), Bp = B/CS).  Axes 0..k-1 span the CTAs: their
+// butterflies read and write the other CTAs' shared memory (DSMEM), each CTA
+// taking an equal share of the groups; axes k..b-1 are local to each part.
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+template <typename T, int Q>
+__global__ void __launch_bounds__(512) gwht_cluster_kernel(c2<T>* __restrict__ data,
+                                                           const int64_t* __restrict__ row_off, int q, int b, int k,
+                                                           int CS, T divisor) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char smem[];
+  uint64_t* mbar = reinterpret_cast<uint64_t*>(smem);
+  int* status = reinterpret_cast<int*>(smem + 8);
+  c2<T>* tw = reinterpret_cast<c2<T>*>(smem + 16);
+  c2<T>* part = tw + QSFT_MAX_Q;
+  const int rank = (int)cluster.block_rank();
+  const int64_t row = blockIdx.x / CS;
+  int Bp = 1;
+  for (int i = k; i < b; ++i) Bp *= q;
+  c2<T>* __restrict__ x = data + __ldg(row_off + row) + (int64_t)rank * Bp;
+  const uint32_t bytes = (uint32_t)Bp * (uint32_t)sizeof(c2<T>);
+  // the TMA engine moves the part when source, destination and size are 16-byte aligned
+  const bool bulk = ((reinterpret_cast<uintptr_t>(x) | bytes) & 15) == 0;
+  if (threadIdx.x == 0) {
+    *status = 1;
+    if (bulk) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(mbar)) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(mbar)), "r"(bytes)
+                   : "memory");
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+              smem_addr(part)),
+          "l"(x), "r"(bytes), "r"(smem_addr(mbar))
+          : "memory");
+    }
+  }
+  if (threadIdx.x < q) {
+    const double2 w = root_of_unity(threadIdx.x, q);
+    tw[threadIdx.x] = cmake<c2<T>>(w.x, -w.y);
+  }
+  if (bulk) {
+    __syncthreads();  // barrier initialised before anyone waits on it
+    bool done = false;
+    // bounded wait; on a timeout wait once more (bounded) so that the copy is not
+    // left writing into shared memory this CTA is about to give up
+    for (int attempt = 0; attempt < 2 && !done; ++attempt) {
+      for (long long i = 0; i < (1ll << 22) && !done; ++i) {
+        uint32_t okp;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], 0;\n\tselp.u32 %0, 1, 0, "
+            "p;\n}\n"
+            : "=r"(okp)
+            : "r"(smem_addr(mbar))
+            : "memory");
+        done = okp != 0;
+      }
+      if (!done && threadIdx.x == 0) *status = 0;  // the row is left untouched
+    }
+  } else {
+    for (int e = threadIdx.x; e < Bp; e += blockDim.x) part[e] = x[e];
+  }
+  cluster.sync();
+  // ---- axes spanning the cluster
+  const int ngroups = (CS / q) * Bp;  // per axis
+  const int per = ngroups / CS;
+  int cstride = CS;                   // stride of digit a in CTA-index units
+  for (int a = 0; a < k; ++a) {
+    cstride /= q;
+    for (int gi = threadIdx.x; gi < per; gi += blockDim.x) {
+      const int G = rank * per + gi;
+      const int g = G % Bp;            // local index
+      const int ch = G / Bp;            // CTA index with digit a removed
+      const int lo = ch % cstride, hi = ch / cstride;
+      const int cta0 = hi * cstride * q + lo;
+      c2<T> v[Q > 0 ? Q : QSFT_MAX_Q];
+      for (int m = 0; m < q; ++m)
+        v[m] = *cluster.map_shared_rank(part + g, cta0 + m * cstride);
+      if constexpr (Q > 0) {
+        dft_small<c2<T>, Q>(v, tw);
+      } else {
+        c2<T> y[QSFT_MAX_Q];
+        for (int kk = 0; kk < q; ++kk) {
+          c2<T> acc = v[0];
+          int idx = 0;
+          for (int m = 1; m < q; ++m) {
+            idx += kk;
+            if (idx >= q) idx -= q;
+            acc = cadd(acc, cmul(v[m], tw[idx]));
+          }
+          y[kk] = acc;
+        }
+        for (int kk = 0; kk < q; ++kk) v[kk] = y[kk];
+      }
+      for (int m = 0; m < q; ++m) *cluster.map_shared_rank(part + g, cta0 + m * cstride) = v[m];
+    }
+    cluster.sync();
+  }
+  // ---- local axes
+  int stride = Bp;
+  for (int a = k; a < b; ++a) {
+    stride /= q;
+    if constexpr (Q > 0) axis_pass_fixed<T, Q>(part, Bp, stride, tw);
+    else axis_pass_generic<T>(part, Bp, stride, q, tw);
+    __syncthreads();
+  }
+  if (bulk) {
+    for (int e = threadIdx.x; e < Bp; e += blockDim.x) {
+      c2<T> v = part[e];
+      v.x = v.x / divisor;
+      v.y = v.y / divisor;
+      part[e] = v;
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    __syncthreads();
+    if (threadIdx.x == 0 && *status) {
+      asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(x), "r"(smem_addr(part)),
+                   "r"(bytes)
+                   : "memory");
+      asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+      asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // smem must outlive the copy's reads
+    }
+  } else {
+    for (int e = threadIdx.x; e < Bp; e += blockDim.x) {
+      c2<T> v = part[e];
+      v.x = v.x / divisor;
+      v.y = v.y / divisor;
+      x[e] = v;
+    }
+  }
+}
+
+// cluster size for a row of q^b values of es bytes, or 0 when the row fits one
+// CTA (<= 48 KB) or no q^k <= 8 brings a part under 64 KB
+static int cluster_split(int q, int b, size_t es, int* kout) {
+  int64_t B = 1;
+  for (int i = 0; i < b; ++i) B *= q;
+  if ((size_t)B * es <= 48 * 1024) return 0;
+  int cs = 1;
+  for (int k = 1; k < b; ++k) {
+    cs *= q;
+    if (cs > 8) return 0;
+    if ((size_t)(B / cs) * es <= 64 * 1024) {
+      *kout = k;
+      return cs;
+    }
+  }
+  return 0;
+}
+
+template <typename T, int Q>
+static int launch_cluster(c2<T>* data, const int64_t* row_off, int64_t nrows, int q, int b, int k, int CS,
+                          T divisor, cudaStream_t st) {
+  int64_t Bp = 1;
+  for (int i = k; i < b; ++i) Bp *= q;
+  const size_t sm = 16 + (size_t)(Bp + QSFT_MAX_Q) * sizeof(c2<T>);
+  auto kern = gwht_cluster_kernel<T, Q>;
+  if (!ensure_smem((const void*)kern, (int)sm)) return QSFT_ERR_CUDA;
+  if (nrows * CS > 0x7fffffffLL) return QSFT_ERR_TOO_LARGE;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(nrows * CS));
+  cfg.blockDim = dim3(Bp >= 4096 ? 512 : 256);
+  cfg.dynamicSmemBytes = sm;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, kern, data, row_off, q, b, k, CS, divisor) != cudaSuccess) return QSFT_ERR_CUDA;
+  QSFT_CUDA_CHECK_LAUNCH();
+  return QSFT_OK;
+}
+
 struct Pass {
   int a0, a1, TI, NO;
 };
@@ -186,8 +370,7 @@ static int launch_pass(c2<T>* data, const int64_t* row_off, int64_t nrows, int q
   const int nel = p.NO * mid * p.TI;
   const size_t sm = (size_t)(nel + QSFT_MAX_Q) * sizeof(c2<T>);
   auto kern = gwht_pass_kernel<T, Q>;
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm) != cudaSuccess)
-    return QSFT_ERR_CUDA;
+  if (!ensure_smem((const void*)kern, (int)sm)) return QSFT_ERR_CUDA;
   const int threads = nel >= 4096 ? 512 : (nel >= 1024 ? 256 : 128);
   const int64_t grid = nrows * tiles_per_row;
   if (grid > 0x7fffffffLL) return QSFT_ERR_TOO_LARGE;
@@ -206,6 +389,17 @@ static int run_gwht(int q, int b, void* data, const int64_t* row_off, int64_t nr
   if (np <= 0) return QSFT_ERR_TOO_LARGE;
   c2<T>* d = reinterpret_cast<c2<T>*>(data);
   const T div = (T)ipow(q, b);
+  int k = 0;
+  const int CS = cluster_split(q, b, es, &k);
+  if (CS > 0) {
+    switch (q) {
+      case 2: return launch_cluster<T, 2>(d, row_off, nrows, q, b, k, CS, div, st);
+      case 3: return launch_cluster<T, 3>(d, row_off, nrows, q, b, k, CS, div, st);
+      case 4: return launch_cluster<T, 4>(d, row_off, nrows, q, b, k, CS, div, st);
+      case 5: return launch_cluster<T, 5>(d, row_off, nrows, q, b, k, CS, div, st);
+      default: return launch_cluster<T, 0>(d, row_off, nrows, q, b, k, CS, div, st);
+    }
+  }
   for (int i = 0; i < np; ++i) {
     const T dv = (i == np - 1) ? div : (T)1;
     int rc;

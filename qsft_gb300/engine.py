@@ -23,9 +23,19 @@ TC_SUB_N = 128    # support entries per MMA sub-tile
 TC_SMEM_TARGET = 110 * 1024   # two CTAs per SM
 
 
-def tc_smem_bytes(npad, smax, max_q, table_bytes=0):
+def tc_entry_bytes(qs):
+    """Table bytes per support entry of the tensor-core kernel: a pair table
+    (q*q entries per two support entries) when every job has the same q in {2, 4}."""
+    qs = set(qs)
+    if len(qs) == 1 and next(iter(qs)) in (2, 4):
+        q = next(iter(qs))
+        return q * q * 4
+    return max(qs) * 8
+
+
+def tc_smem_bytes(npad, smax, entry_bytes, table_bytes=0):
     """Shared memory of the tensor-core evaluation kernel (mirrors eval_tc.cu)."""
-    return max(2048 + 128 * npad * 2 + smax * npad * 2 + smax * max_q * 8 + table_bytes, 80 * 1024)
+    return max(2048 + 128 * npad * 2 + smax * npad * 2 + smax * entry_bytes + table_bytes, 80 * 1024)
 MAX_ITER = 15     # qsft/qsft.py:142
 
 _ROOTS = {}
@@ -141,12 +151,13 @@ class Batch:
                     gf_parts.append(tb)
                     off_gf += tb.size
                 jb.rs_s, jb.rs_t, jb.rs_gf_off = sp.rs.s, sp.rs.t, gf_index[key]
+            # 16-byte aligned sub-arrays (word loads of the delay rows in detection)
             jb.off_M = off_i8
-            off_i8 += sp.M.size
+            off_i8 = (off_i8 + sp.M.size + 15) & ~15
             jb.off_D = off_i8
-            off_i8 += sp.D.size
+            off_i8 = (off_i8 + sp.D.size + 15) & ~15
             jb.off_K = off_i8
-            off_i8 += 0 if sp.K is None else sp.K.size
+            off_i8 = (off_i8 + (0 if sp.K is None else sp.K.size) + 15) & ~15
             jb.off_A = off_a
             off_a += 0 if sp.A is None else sp.A.size
             jb.off_U = off_u
@@ -167,14 +178,15 @@ class Batch:
         # tensor-core evaluation: K extent, support chunk, work items
         maxn = max(sp.n for sp in specs)
         self.tc_npad = 32 if maxn <= 32 else (64 if maxn <= 64 else 128)
-        maxq = max(sp.q for sp in specs)
+        self.tc_entry_bytes = tc_entry_bytes([sp.q for sp in specs])
         self.tc_table_bytes = max(sp.C * (sp.b * sp.q + sp.R * sp.P) * self.tc_npad for sp in specs)
         smax = TC_SUB_N
-        while tc_smem_bytes(self.tc_npad, smax + TC_SUB_N, maxq, self.tc_table_bytes) <= TC_SMEM_TARGET:
+        while tc_smem_bytes(self.tc_npad, smax + TC_SUB_N, self.tc_entry_bytes,
+                            self.tc_table_bytes) <= TC_SMEM_TARGET:
             smax += TC_SUB_N
         self.tc_smax = smax
         # the tensor-core kernel needs its tables and one 128-entry support chunk in shared memory
-        self.tc_ok = tc_smem_bytes(self.tc_npad, smax, maxq, self.tc_table_bytes) <= 227 * 1024
+        self.tc_ok = tc_smem_bytes(self.tc_npad, smax, self.tc_entry_bytes, self.tc_table_bytes) <= 227 * 1024
         tc_prefix = [0]
         self.tc_needs_zero = False
         for sp in specs:
@@ -215,6 +227,10 @@ class Batch:
         self.ball_k = z(self.total_balls * self.kstride, torch.uint8)
         self.ball_sum = z(self.total_balls * 2, torch.float64)
         self.ball_cnt = z(self.total_balls, torch.int32)
+        self.bin_status = z(self.total_bins, torch.uint8)
+        self.bin_stamp = z(self.total_bins, torch.int32)
+        self.dirty = z(2 * self.total_bins, torch.int32)
+        self.cand = z(self.total_bins, torch.int32)
         self.out_k = z(self.total_balls * self.kstride, torch.uint8)
         self.out_val = z(self.total_balls * 2, torch.float64)
         self.out_cnt = z(self.total_balls, torch.int32)
@@ -245,8 +261,13 @@ class Batch:
         p.kbuf, p.rho, p.tab_key, p.tab_best = ptr(self.kbuf), ptr(self.rho), ptr(self.tab_key), ptr(self.tab_best)
         p.uniq, p.ball_tab, p.ball_k = ptr(self.uniq), ptr(self.ball_tab), ptr(self.ball_k)
         p.ball_sum, p.ball_cnt, p.ctrl = ptr(self.ball_sum), ptr(self.ball_cnt), ptr(self.ctrl)
+        p.bin_status, p.bin_stamp = ptr(self.bin_status), ptr(self.bin_stamp)
+        p.dirty, p.cand = ptr(self.dirty), ptr(self.cand)
+        self.done_count = z(1, torch.int32)
+        p.done_count = ptr(self.done_count)
         p.tc_prefix, p.total_tc_work = ptr(self.tc_prefix), self.tc_prefix_host[-1]
         p.tc_smax, p.tc_npad, p.tc_table_bytes = self.tc_smax, self.tc_npad, self.tc_table_bytes
+        p.tc_entry_bytes = self.tc_entry_bytes
         p.status = ptr(self.status)
         self.plan = p
 
@@ -321,6 +342,40 @@ class Batch:
         check(self.lib.qsft_peel_init(ctypes.byref(self.plan), sh), "qsft_peel_init")
         check(self.lib.qsft_peel_run(ctypes.byref(self.plan), int(max_iter), sh), "qsft_peel_run")
 
+    # ------------------------------------------------------------ whole step
+    def step(self, max_iter=None, stream=None):
+        """eval -> gwht -> noise -> peel -> collect, issued on the stream."""
+        self.eval(stream)
+        self.gwht(stream)
+        self.add_noise(stream)
+        self.peel(self.max_iter if max_iter is None else max_iter, stream)
+        self.collect_async(stream)
+
+    def capture(self, max_iter=None):
+        """Record one step into a CUDA graph (replayed by run()); the graph reads
+        the workspace buffers, so later load()s need no re-capture."""
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(side):
+            self.step(max_iter)            # warm-up: kernel attributes, lazy loads
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        torch.cuda.synchronize(self.device)
+        g = torch.cuda.CUDAGraph()
+        l0 = self.lib.qsft_launch_count()
+        with torch.cuda.graph(g):
+            self.step(max_iter)
+        self.graph_launches = self.lib.qsft_launch_count() - l0
+        self.graph = g
+        return g
+
+    def run(self):
+        """One step: graph replay when captured, else direct launches."""
+        g = getattr(self, "graph", None)
+        if g is not None:
+            g.replay()
+        else:
+            self.step()
+
     def collect_async(self, stream=None):
         check(self.lib.qsft_collect(ctypes.byref(self.plan), ctypes.c_void_p(self.out_k.data_ptr()),
                                     ctypes.c_void_p(self.out_val.data_ptr()), ctypes.c_void_p(self.out_cnt.data_ptr()),
@@ -338,11 +393,13 @@ class Batch:
         self.meta_host.copy_(self.meta)   # synchronises with the stream
         return self.meta_host.numpy()
 
-    def results(self, stream=None):
+    def results(self, stream=None, collected=False):
         """Per job: (keys (m, n) int64, values complex128 (m,), counts int32 (m,), ctrl).
 
-        Two device->host copies: the metadata, then the used rows of the output."""
-        self.collect_async(stream)
+        Two device->host copies: the metadata, then the used rows of the output.
+        collected=True skips the collect launch (a captured step already did it)."""
+        if not collected:
+            self.collect_async(stream)
         meta = self._read_meta()
         J = self.njobs
         total = int(meta[0])

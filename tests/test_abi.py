@@ -95,4 +95,4 @@ def test_gpu_entry_points_reject_bad_arguments_without_launching(lib):
     assert lib.qsft_rs_decode(5, 3, 17, 100, None, None, 1, None, None) == -1   # t > 16
     assert lib.qsft_add_bins(4, None, None, -1, None) == -1
     assert lib.qsft_eval_cosets(None, None) == -1
-    assert lib.qsft_peel_iteration(None, None) == -1
+    assert lib.qsft_peel_iteration(None, 1, None) == -1

@@ -36,7 +36,7 @@ def test_gwht_matches_reference_pins(cuda, prec):
 
 
 @pytest.mark.parametrize("prec", PRECS)
-@pytest.mark.parametrize("q,b", [(2, 14), (3, 9), (4, 8), (5, 6), (7, 4), (20, 3), (20, 4), (16, 4), (32, 3)])
+@pytest.mark.parametrize("q,b", [(2, 14), (2, 15), (3, 9), (4, 7), (4, 8), (5, 6), (7, 4), (8, 5), (20, 3), (20, 4), (16, 4), (32, 3)])
 def test_gwht_sizes_vs_oracle(cuda, prec, q, b):
     """Single-pass and multi-pass (rows above the shared-memory budget) transforms."""
     import torch
@@ -251,3 +251,26 @@ def test_eval_tensor_cores_vs_cuda_cores_and_oracle(cuda, shapes):
             X = O.coset_points(sp.M[g], sp.D[g][0], sp.q).T
             want = O.eval_points(X, sp.K.T, sp.A, sp.q)
             assert rel_err(a[g, 0], want) < 2e-6 * np.sqrt(sp.S)
+
+
+def test_transform_batch_replays_new_inputs(cuda):
+    """transform_batch captures one CUDA graph per layout; a second batch with
+    the same layout but different inputs must give the results of a direct run."""
+    from qsft_gb300.engine import Batch
+    from qsft_gb300.serve import random_request, transform_batch
+    np.random.seed(21)
+    reqs_a = [random_request(4, 12, 5, 60, C=3, R=2, snr_db=20.0) for _ in range(3)]
+    reqs_b = [random_request(4, 12, 5, 60, C=3, R=2, snr_db=20.0) for _ in range(3)]
+    out_a = transform_batch(reqs_a)
+    out_b = transform_batch(reqs_b)
+    for reqs, out in ((reqs_a, out_a), (reqs_b, out_b)):
+        bt = Batch([r.spec() for r in reqs], precision="fp32")
+        bt.step()
+        direct = bt.results(collected=True)
+        for (k, v, _, _), res in zip(direct, out):
+            d1 = {tuple(x): y for x, y in zip(k.tolist(), v)}
+            d2 = {tuple(x): y for x, y in zip(res.keys.tolist(), res.values)}
+            assert set(d1) == set(d2) and len(d1) > 0
+            assert max(abs(d1[x] - d2[x]) for x in d1) < 1e-5
+        truth = [set(map(tuple, r.locq.T.tolist())) for r in reqs]
+        assert all(len(set(map(tuple, res.keys.tolist())) & t) >= 58 for res, t in zip(out, truth))
