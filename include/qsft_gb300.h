@@ -269,6 +269,31 @@ int qsft_collect(const qsft_plan* plan, uint8_t* out_k, double* out_val, int32_t
 int qsft_rs_decode(int q, int s, int t, int n, const int32_t* gf_tables, const uint8_t* syms,
                    int64_t nrows, uint8_t* k_out, qsft_stream_t stream);
 
+/* ---- peeling without device allocation ------------------------------------ */
+#define QSFT_NOALLOC_MAX_BINS 16384  /* largest C * q^b of a qsft_peel_noalloc job       */
+#define QSFT_NOALLOC_KSTRIDE 32      /* out_k row bytes; the job's n must be <= 32        */
+/*
+ * No counterpart in the reference: the peeling loop of qsft_peel_init +
+ * qsft_peel_run + qsft_collect for ONE job, for callers that cannot allocate
+ * device memory -- code being captured into a CUDA graph (cudaMalloc and
+ * cudaFree cannot be captured), serving threads that must not stall on
+ * cudaMalloc's device-wide synchronisation, plugin hosts that own every
+ * buffer.  All scratch (hash tables, result store, lists, roots table, control
+ * record) lives in a statically sized device array inside the library (about
+ * 2.9 MB, held by every GPU that loads the library until the process exits),
+ * so the call allocates nothing.  `job` is a host record (offsets off_M/off_D
+ * into i8, off_U into U; qsft_workspace_layout's fields are filled in by the
+ * call); U holds the job's bins and is peeled in place.  Results as
+ * qsft_collect, rows of QSFT_NOALLOC_KSTRIDE bytes; max_out must be at least
+ * C*q^b + 64.  Limits: C*q^b <= QSFT_NOALLOC_MAX_BINS, n <= 32, else
+ * QSFT_ERR_TOO_LARGE.  Every call shares the one array: calls that overlap on
+ * the GPU race; serialise them.  The first call on a device looks up the
+ * array's address with that device current; make it before any stream capture.
+ */
+int qsft_peel_noalloc(int prec, const qsft_job* job, const int8_t* i8, void* U, const int32_t* gf_tables,
+                      uint8_t* out_k, double* out_val, int32_t* out_cnt, int64_t* out_total, int32_t max_out,
+                      qsft_stream_t stream);
+
 /*
  * Scratch sizes for a batch: given the jobs' (q, n, b, C, B) on the host,
  * writes the counts of bins, hash slots, balls and the kstride, and fills the

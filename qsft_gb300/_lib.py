@@ -20,6 +20,8 @@ MAX_RS_T = 16
 MAX_GF = 4096
 TC_TILES = 16     # QSFT_TC_TILES
 TC_TILE_M = 128
+NOALLOC_MAX_BINS = 16384   # QSFT_NOALLOC_MAX_BINS
+NOALLOC_KSTRIDE = 32       # QSFT_NOALLOC_KSTRIDE
 TC_SUB_N = 128
 
 # exported symbols, in header order
@@ -27,7 +29,7 @@ SYMBOLS = [
     "qsft_abi_version", "qsft_status_string", "qsft_built_arch", "qsft_launch_count", "qsft_eval_cosets",
     "qsft_eval_cosets_tc", "qsft_eval_points",
     "qsft_gwht", "qsft_add_noise_philox", "qsft_add_bins", "qsft_peel_init", "qsft_peel_iteration",
-    "qsft_peel_run", "qsft_collect", "qsft_rs_decode", "qsft_workspace_layout",
+    "qsft_peel_run", "qsft_collect", "qsft_rs_decode", "qsft_peel_noalloc", "qsft_workspace_layout",
 ]
 
 
@@ -113,6 +115,7 @@ def load():
         "qsft_peel_run": ([plan_p, i32, vp], i32),
         "qsft_collect": ([plan_p, vp, vp, vp, vp, vp, vp], i32),
         "qsft_rs_decode": ([i32, i32, i32, i32, vp, vp, i64, vp, vp], i32),
+        "qsft_peel_noalloc": ([i32, ctypes.POINTER(QsftJob), vp, vp, vp, vp, vp, vp, vp, i32, vp], i32),
         "qsft_workspace_layout": ([ctypes.POINTER(QsftJob), i32, ctypes.POINTER(i64), ctypes.POINTER(i64),
                                    ctypes.POINTER(i64), ctypes.POINTER(ctypes.c_int32)], i32),
     }
