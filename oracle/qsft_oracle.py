@@ -167,18 +167,23 @@ def gwht(x, q, b):
     return np.reshape(_fft.fftn(np.reshape(x, [q] * b)) / (q ** b), [q ** b])
 
 
-def subsample_qsft(Ms, Ds, q, eval_fn):
-    """Us[c][r] = P x B bins for every (group, repeat) (qsft/input_signal_subsampled.py:107-155)."""
-    Us = []
+def subsample_qsft(Ms, Ds, q, eval_fn, all_bs=None):
+    """Us[c][r] = P x B bins for every (group, repeat) (qsft/input_signal_subsampled.py:107-155).
+    With all_bs, returns {b: Us} where the sub-transform for b takes every
+    q^(b_max-b)-th sample (_compute_subtransform, :264-266)."""
+    per_b = {}
     for M, Dlist in zip(Ms, Ds):
-        row = []
-        b = M.shape[1]
+        bmax = M.shape[1]
+        bs = all_bs or [bmax]
+        rows = {bb: [] for bb in bs}
         for D in Dlist:
             pts = [coset_points(M, d, q) for d in D]
-            samples = eval_fn(np.concatenate([p.T for p in pts], axis=0)).reshape(len(D), q ** b)
-            row.append(np.array([gwht(s, q, b) for s in samples]))
-        Us.append(row)
-    return Us
+            samples = eval_fn(np.concatenate([p.T for p in pts], axis=0)).reshape(len(D), q ** bmax)
+            for bb in bs:
+                rows[bb].append(np.array([gwht(s[::q ** (bmax - bb)], q, bb) for s in samples]))
+        for bb in bs:
+            per_b.setdefault(bb, []).append(rows[bb])
+    return per_b if all_bs else per_b[Ms[0].shape[1]]
 
 
 def get_MDU_perm(C_have, R_have, C, R):
@@ -308,9 +313,12 @@ class OracleSignal:
         self.num_subsample = qa["num_subsample"]
         self.num_repeat = qa["num_repeat"]
         self.Ms, self.Ds = get_Ms_and_Ds(n, q, **qa)
+        self.all_bs = qa.get("all_bs", [self.b])
         if not skip_sampling:
-            self.Us = subsample_qsft(self.Ms, self.Ds, q,
-                                     lambda X: eval_points(X, self.locq, self.strengths, q, threads=eval_threads))
+            self.Us_b = subsample_qsft(self.Ms, self.Ds, q,
+                                       lambda X: eval_points(X, self.locq, self.strengths, q, threads=eval_threads),
+                                       all_bs=self.all_bs)
+            self.Us = self.Us_b[self.b]
 
     def get_source_parity(self):  # qsft/input_signal_subsampled.py:268-269
         return self.Ds[0][0].shape[0]
@@ -322,7 +330,8 @@ class OracleSignal:
         ci, ri = get_MDU_perm(self.num_subsample, self.num_repeat, C, R)
         Ms = [self.Ms[i][:, :b] for i in ci]
         Ds = [[self.Ds[i][j] for j in ri] for i in ci]
-        Us = [[self.Us[i][j][:, ::self.q ** (self.b - b)] if b != self.b else self.Us[i][j] for j in ri] for i in ci]
+        src = self.Us if b == self.b else self.Us_b[b]
+        Us = [[src[i][j] for j in ri] for i in ci]
         out = []
         for row in Us:
             out.append([u + bin_noise(self.noise_sd, self.q, b, u.shape) for u in row])

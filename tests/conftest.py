@@ -36,9 +36,17 @@ def load_golden(name):
 
 
 def case_query_args(z):
-    return dict(query_method=str(z["query_method"]), num_subsample=int(z["C"]),
-                delays_method_source=str(z["src"]), subsampling_method="qsft",
-                delays_method_channel=str(z["ch"]), num_repeat=int(z["R"]), b=int(z["b"]))
+    qa = dict(query_method=str(z["query_method"]), num_subsample=int(z["C"]),
+              delays_method_source=str(z["src"]), subsampling_method="qsft",
+              delays_method_channel=str(z["ch"]), num_repeat=int(z["R"]), b=int(z["b"]))
+    if "all_bs" in z and len(z["all_bs"]) > 1:
+        qa["all_bs"] = [int(x) for x in z["all_bs"]]
+    return qa
+
+
+def transform_b(z):
+    """b of the QSFT call (smaller than the signal's b for all_bs cases)."""
+    return int(z["transform_b"]) if "transform_b" in z else int(z["b"])
 
 
 def golden_dict(z):

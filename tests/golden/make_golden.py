@@ -91,6 +91,8 @@ CASES = {
     "q5n10b3_nso_clean": dict(q=5, n=10, b=3, S=30, C=3, R=1, src="identity", ch="nso", snr=None, seed=5, full=True),
     "q4n10b4_simple_nso": dict(q=4, n=10, b=4, S=40, C=2, R=2, src="identity", ch="nso", snr=20, seed=6, full=True,
                                query_method="simple"),
+    "q4n10b5_allbs_b4_nso": dict(q=4, n=10, b=5, S=30, C=3, R=2, src="identity", ch="nso", snr=20, seed=8, full=False,
+                                 all_bs=[4, 5], transform_b=4),
     "cfg2_q4n20b7_nso_10db": dict(q=4, n=20, b=7, S=1000, C=3, R=2, src="identity", ch="nso", snr=10, seed=0, full=False),
     "cfg3_q20n10b3_nso_20db": dict(q=20, n=10, b=3, S=500, C=3, R=3, src="identity", ch="nso", snr=20, seed=0, full=False),
 }
@@ -106,6 +108,9 @@ def run_case(name, p):
     qa = dict(query_method=p.get("query_method", "complex"), num_subsample=C,
               delays_method_source=p["src"], subsampling_method="qsft",
               delays_method_channel=p["ch"], num_repeat=R, b=b)
+    if "all_bs" in p:
+        qa["all_bs"] = list(p["all_bs"])
+    tb = p.get("transform_b", b)
     np.random.seed(p["seed"])
     t0 = time.time()
     sig = get_random_subsampled_signal(n=n, q=q, sparsity=S, a_min=1, a_max=10, noise_sd=nsd, query_args=qa)
@@ -139,7 +144,7 @@ def run_case(name, p):
     qmod.singleton_detection = rec_sd
     try:
         res = QSFT(num_subsample=C, num_repeat=R, reconstruct_method_source=p["src"],
-                   reconstruct_method_channel=p["ch"], b=b).transform(sig, report=True, sort=True)
+                   reconstruct_method_channel=p["ch"], b=tb).transform(sig, report=True, sort=True)
     finally:
         qmod.singleton_detection = orig_sd
     t2 = time.time()
@@ -151,7 +156,8 @@ def run_case(name, p):
     nmse = sum(abs(tw.get(k, 0) - g.get(k, 0)) ** 2 for k in set(tw) | set(g)) / sum(abs(v) ** 2 for v in tw.values())
 
     out = dict(
-        q=q, n=n, b=b, S=S, C=C, R=R, seed=p["seed"], noise_sd=nsd,
+        q=q, n=n, b=b, S=S, C=C, R=R, seed=p["seed"], noise_sd=nsd, transform_b=tb,
+        all_bs=np.array(qa.get("all_bs", [b]), dtype=np.int64),
         src=p["src"], ch=p["ch"], query_method=qa["query_method"],
         locq=np.asarray(sig.locq, dtype=np.int64),
         strengths=np.asarray(list(tw.values()), dtype=np.complex128),

@@ -12,7 +12,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from conftest import case_query_args, golden_cases, golden_dict, load_golden
+from conftest import case_query_args, golden_cases, golden_dict, load_golden, transform_b
 
 pytestmark = pytest.mark.gpu
 
@@ -83,7 +83,7 @@ def _run_product(z, prec, noise="host"):
     np.random.seed(int(z["seed"]))
     sig = Q.get_random_subsampled_signal(n=n, q=q, sparsity=S, a_min=1, a_max=10, noise_sd=float(z["noise_sd"]),
                                          query_args=case_query_args(z), precision=prec, noise=noise)
-    res = Q.QSFT(num_subsample=C, num_repeat=R, b=b, reconstruct_method_source=str(z["src"]),
+    res = Q.QSFT(num_subsample=C, num_repeat=R, b=transform_b(z), reconstruct_method_source=str(z["src"]),
                  reconstruct_method_channel=str(z["ch"])).transform(sig, report=True, sort=True)
     return sig, res
 
@@ -274,3 +274,75 @@ def test_transform_batch_replays_new_inputs(cuda):
             assert max(abs(d1[x] - d2[x]) for x in d1) < 1e-5
         truth = [set(map(tuple, r.locq.T.tolist())) for r in reqs]
         assert all(len(set(map(tuple, res.keys.tolist())) & t) >= 58 for res, t in zip(out, truth))
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_config4_coded_full_size(cuda, prec):
+    """q=5, n=100, b=5, C=3, RS-coded delays t=8, S=200 of Hamming weight <= 8,
+    20 dB: the RS path has no reference run (galois), so ground truth."""
+    import qsft_gb300 as Q
+    q, n, b, S, t = 5, 100, 5, 200, 8
+    qa = dict(query_method="complex", num_subsample=3, delays_method_source="coded", subsampling_method="qsft",
+              delays_method_channel="nso", num_repeat=1, b=b, t=t)
+    np.random.seed(0)
+    sig = Q.get_random_subsampled_signal(n=n, q=q, sparsity=S, a_min=1, a_max=10, noise_sd=O.noise_sd_for_snr(S, 20),
+                                         query_args=qa, max_weight=t, precision=prec)
+    res = Q.QSFT(num_subsample=3, num_repeat=1, b=b, reconstruct_method_source="coded", reconstruct_method_channel="nso",
+                 source_decoder=Q.get_reed_solomon_dec(n, t, q)).transform(sig, report=True)
+    assert set(res["gwht"]) == set(sig.signal_w)
+    assert O.nmse(sig.signal_w, res["gwht"]) < 1e-4
+    assert res["n_samples"] == 3 * sig.get_source_parity() * q ** b
+    assert res["max_hamming_weight"] <= t
+
+
+def test_folder_cache_round_trip(cuda, tmp_path):
+    """folder=: Ms/Ds and the sub-transforms are saved on the first build and
+    loaded on the second (qsft/input_signal_subsampled.py:92-155)."""
+    import qsft_gb300 as Q
+    qa = dict(query_method="complex", num_subsample=3, delays_method_source="identity", subsampling_method="qsft",
+              delays_method_channel="nso", num_repeat=2, b=4)
+    out = []
+    for _ in range(2):
+        np.random.seed(3)
+        sig = Q.get_random_subsampled_signal(n=10, q=4, sparsity=30, a_min=1, a_max=10, noise_sd=0.5,
+                                             query_args=dict(qa), folder=str(tmp_path))
+        np.random.seed(99)
+        out.append(Q.QSFT(num_subsample=3, num_repeat=2, b=4, reconstruct_method_source="identity",
+                          reconstruct_method_channel="nso").transform(sig))
+    assert (tmp_path / "Ms_and_Ds.pickle").is_file()
+    assert set(out[0]) == set(out[1]) and len(out[0]) >= 28
+    assert max(abs(out[0][k] - out[1][k]) for k in out[0]) < 1e-6
+
+
+def test_generic_plugin_subsample(cuda):
+    """A user SubsampledSignal that only implements subsample(query_indices) on
+    the host: sub-transforms and peeling on the GPU give the synthetic path's result."""
+    import qsft_gb300 as Q
+    from qsft_gb300.utils import dec_to_qary_vec
+
+    class HostSignal(Q.SubsampledSignal):
+        def __init__(self, locq, strengths, **kw):
+            self.locq, self.strengths = locq, strengths
+            self.noise_sd = kw["noise_sd"]     # read by transform's cutoff (qsft/qsft.py:125)
+            super().__init__(**kw)
+
+        def subsample(self, query_indices):
+            X = dec_to_qary_vec(np.asarray(query_indices), self.q, self.n).T
+            return np.exp(2j * np.pi * (X @ self.locq) / self.q) @ self.strengths
+
+    qa = dict(query_method="complex", num_subsample=3, delays_method_source="identity", subsampling_method="qsft",
+              delays_method_channel="identity", num_repeat=1, b=4)
+    np.random.seed(12)
+    syn = Q.get_random_subsampled_signal(n=9, q=4, sparsity=25, a_min=1, a_max=10, noise_sd=0.0, query_args=dict(qa))
+    np.random.seed(12)
+    _, locq, strengths = Q.generate_signal_w(9, 4, 25, 1, 10, full=False)
+    host = HostSignal(locq, strengths, n=9, q=4, noise_sd=0.0, query_args=dict(qa))
+    host.Ms, host.Ds = syn.Ms, syn.Ds          # same query design (drawn once)
+    host._subsample_qsft()
+    res = []
+    for sig in (syn, host):
+        np.random.seed(5)
+        res.append(Q.QSFT(num_subsample=3, num_repeat=1, b=4, reconstruct_method_source="identity",
+                          reconstruct_method_channel="identity").transform(sig))
+    assert set(res[0]) == set(res[1]) == set(syn.signal_w)
+    assert max(abs(res[0][k] - res[1][k]) for k in res[0]) < 1e-4

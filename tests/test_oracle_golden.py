@@ -4,7 +4,7 @@ import numpy as np
 import pytest
 
 import oracle as O
-from conftest import case_query_args, golden_cases, golden_dict, load_golden
+from conftest import case_query_args, golden_cases, golden_dict, load_golden, transform_b
 
 
 @pytest.mark.parametrize("name", golden_cases(full_only=True))
@@ -91,3 +91,18 @@ def test_gf_tables_are_fields():
         g = O.rs.GF(p, m)
         assert g.poly == O.rs.CONWAY[(p, m)], "Conway polynomial not primitive"
         assert sorted(g.exp[:g.order - 1]) == list(range(1, g.order))
+
+
+def test_oracle_all_bs_matches_reference():
+    """all_bs: the signal is sampled at b=5 and transformed at b=4 from every
+    4th sample (qsft/input_signal_subsampled.py:150-153, 264-266)."""
+    z = load_golden("q4n10b5_allbs_b4_nso")
+    np.random.seed(int(z["seed"]))
+    sig = O.OracleSignal(int(z["n"]), int(z["q"]), int(z["S"]), 1, 10, float(z["noise_sd"]), case_query_args(z))
+    res = O.OracleQSFT(num_subsample=int(z["C"]), num_repeat=int(z["R"]), reconstruct_method_source="identity",
+                       reconstruct_method_channel="nso", b=transform_b(z)).transform(sig, report=True)
+    got = {tuple(int(x) for x in k): v for k, v in res["gwht"].items()}
+    want = golden_dict(z)
+    assert set(got) == set(want)
+    assert max(abs(got[k] - want[k]) for k in want) < 1e-12
+    assert res["n_samples"] == int(z["n_samples"])
