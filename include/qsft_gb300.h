@@ -157,6 +157,22 @@ typedef struct qsft_plan {
                                 * (pair table), else max_q*8                        */
   int32_t pad2_;
   int32_t* status;             /* [1] device word, 0 = ok, else a qsft_status       */
+  /* coset-factored tensor-core evaluation (qsft_eval_cosets_gemm); the gm_*
+   * sizes and counts are filled in by qsft_gemm_layout                         */
+  void* gm_ws;                 /* operand workspace of gm_ws_bytes                  */
+  const int64_t* gm_index;     /* [3*njobs+2]: CTA prefix [njobs+1] | operand-block
+                                * prefix [njobs+1] | byte offset of each job's
+                                * region in gm_ws [njobs]                            */
+  int64_t total_gm_work;       /* CTAs of the GEMM kernel                           */
+  int64_t total_gm_prep;       /* blocks of the operand kernel                      */
+  int64_t gm_ws_bytes;
+  int32_t gm_mt;               /* 128-row MMA tiles per CTA (1, 2 or 4)             */
+  int32_t gm_kps;              /* K entries per support vector: 4 when every q is 2
+                                * or 4 (exact FP16 characters), else 8             */
+  int32_t gm_nw;               /* 32-bit words of packed b-digit vectors (1, 2, 4)  */
+  int32_t gm_npmax;            /* largest N extent: 2*R*P rounded up to 16          */
+  int32_t gm_jt_bytes;         /* shared-memory bytes of the largest j table        */
+  int32_t gm_pad_;
 } qsft_plan;
 
 /* tiles of 128 samples per tensor-core work item */
@@ -192,6 +208,30 @@ int qsft_eval_cosets(const qsft_plan* plan, qsft_stream_t stream);
  * support chunk) are added into U with vector reductions.
  */
 int qsft_eval_cosets_tc(const qsft_plan* plan, qsft_stream_t stream);
+
+/*
+ * Same result as qsft_eval_cosets for FP32 plans, computed as one complex GEMM
+ * per (job, group) on the tensor cores.  With x = M_c l + d and
+ * j_s = M_c^T k_s (mod q),
+ *   U[c][rp][l] = sum_s omega^(<l, j_s>) * (a_s omega^(<d_rp, k_s>))
+ *               = (W C)[l][rp],
+ * W the q^b x S character matrix of the j_s (exact in FP16 for q in {2, 4};
+ * hi + lo FP16 halves otherwise) and C the S x R*P coefficient matrix (hi + lo
+ * FP16 halves of a per-job power-of-two scaling).  An operand kernel builds C
+ * and the j_s into gm_ws; the GEMM kernel generates W tiles in shared memory
+ * and runs tcgen05.mma kind::f16 into tensor memory.  U needs no zeroing.
+ * Needs the plan's gm_* fields from qsft_gemm_layout.
+ */
+int qsft_eval_cosets_gemm(const qsft_plan* plan, qsft_stream_t stream);
+/*
+ * Host-side sizing for qsft_eval_cosets_gemm: from the jobs' shapes (q, n, b,
+ * C, R, P, S, B), fills plan->gm_mt, gm_kps, gm_nw, gm_npmax, gm_jt_bytes,
+ * total_gm_work, total_gm_prep, gm_ws_bytes and index_host[3*njobs+2] (to be
+ * uploaded to plan->gm_index).  QSFT_ERR_TOO_LARGE when a job is outside the
+ * kernel's limits (q > 32, b > 16, 2*R*P > 256, S > 8192): use
+ * qsft_eval_cosets_tc for such batches.
+ */
+int qsft_gemm_layout(const qsft_job* jobs_host, int njobs, qsft_plan* plan, int64_t* index_host);
 
 /*
  * Replaces SyntheticSubsampledSignal.subsample(query_indices)

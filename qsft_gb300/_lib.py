@@ -27,7 +27,7 @@ TC_SUB_N = 128
 # exported symbols, in header order
 SYMBOLS = [
     "qsft_abi_version", "qsft_status_string", "qsft_built_arch", "qsft_launch_count", "qsft_eval_cosets",
-    "qsft_eval_cosets_tc", "qsft_eval_points",
+    "qsft_eval_cosets_tc", "qsft_eval_cosets_gemm", "qsft_gemm_layout", "qsft_eval_points",
     "qsft_gwht", "qsft_add_noise_philox", "qsft_add_bins", "qsft_peel_init", "qsft_peel_iteration",
     "qsft_peel_run", "qsft_collect", "qsft_rs_decode", "qsft_peel_noalloc", "qsft_workspace_layout",
 ]
@@ -82,6 +82,10 @@ class QsftPlan(ctypes.Structure):
         ("tc_prefix", _P), ("total_tc_work", ctypes.c_int64), ("tc_smax", ctypes.c_int32),
         ("tc_npad", ctypes.c_int32), ("min_q", ctypes.c_int32), ("tc_table_bytes", ctypes.c_int32),
         ("tc_entry_bytes", ctypes.c_int32), ("pad2_", ctypes.c_int32), ("status", _P),
+        ("gm_ws", _P), ("gm_index", _P), ("total_gm_work", ctypes.c_int64), ("total_gm_prep", ctypes.c_int64),
+        ("gm_ws_bytes", ctypes.c_int64), ("gm_mt", ctypes.c_int32), ("gm_kps", ctypes.c_int32),
+        ("gm_nw", ctypes.c_int32), ("gm_npmax", ctypes.c_int32), ("gm_jt_bytes", ctypes.c_int32),
+        ("gm_pad_", ctypes.c_int32),
     ]
 
 
@@ -106,6 +110,8 @@ def load():
         "qsft_launch_count": ([], i64),
         "qsft_eval_cosets": ([plan_p, vp], i32),
         "qsft_eval_cosets_tc": ([plan_p, vp], i32),
+        "qsft_eval_cosets_gemm": ([plan_p, vp], i32),
+        "qsft_gemm_layout": ([ctypes.POINTER(QsftJob), i32, plan_p, ctypes.POINTER(i64)], i32),
         "qsft_eval_points": ([i32, i32, i32, i32, vp, i64, vp, vp, vp, vp], i32),
         "qsft_gwht": ([i32, i32, i32, vp, vp, i64, vp], i32),
         "qsft_add_noise_philox": ([plan_p, vp], i32),

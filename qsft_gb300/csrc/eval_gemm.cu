@@ -1,0 +1,512 @@
+// Coset evaluation as a complex GEMM on the 5th-generation tensor cores.
+//
+// The samples of group c are U[rp][l] = f(M_c l + d_rp), l in Z_q^b, with
+// f(x) = sum_s a_s omega^(<x, k_s>) (synthetic_signal.py:100-118 evaluated on
+// the cosets of qsft/input_signal_subsampled.py:183-206).  Because
+//   <M_c l + d, k_s> = <l, j_s> + <d, k_s>  (mod q),  j_s = M_c^T k_s mod q,
+// every coset row is the same character matrix applied to different
+// coefficients:
+//   U[rp][l] = sum_s W[l][s] C[s][rp],   W[l][s] = omega^(<l, j_s>),
+//                                         C[s][rp] = a_s omega^(<d_rp, k_s>).
+// W has q^b rows and S columns, C has S rows and R*P columns: one GEMM per
+// (job, group) with K = S replaces S table lookups per sample.
+//
+// Precision.  For q in {2, 4} the characters are 0, +-1, +-i: exact in FP16.
+// Other q use W = W_hi + W_lo (FP16 halves of the FP64 root).  C is scaled by
+// a power of two per job (largest |a_s| -> [2^13, 2^14)) and split into
+// C_hi + C_lo FP16 halves, so each product carries ~22 significant bits; the
+// tensor core multiplies exactly and accumulates in FP32.
+//
+// Real GEMM layout.  Complex products become real ones over K entries per
+// support vector (KPS):
+//   KPS = 4 (q in {2, 4}):  A[l][4s..4s+3] = [Wr, Wi, Wr, Wi]
+//     B[4s..4s+3][2rp]   = [Chr, -Chi, Clr, -Cli]   (real part of W C)
+//     B[4s..4s+3][2rp+1] = [Chi,  Chr, Cli,  Clr]   (imaginary part)
+//   KPS = 8:                A[l][8s..8s+7] = [Whr, Whi, Whr, Whi, Wlr, Wli, Wlr, Wli]
+//     B rows repeat the four KPS = 4 rows twice.
+// N = 2*R*P rounded up to 16 (<= 256).  An operand kernel writes B (and the
+// packed j_s digits) into a workspace in the exact shared-memory image of each
+// 32-entry K chunk, so the GEMM kernel streams it with one bulk copy per
+// stage.  The GEMM kernel generates A in shared memory from the row's digits
+// (two dp4a per support vector for b <= 8) and issues tcgen05.mma kind::f16
+// (M = 128, N, K = 16) into tensor memory.
+//
+// CTA: MT tiles of 128 rows (one producer thread per row, MT*128 threads),
+// one MMA-issuing warp and one bulk-copy warp.  Stages of (A, B) chunks in a
+// ring guarded by mbarriers: bfull (bulk copy landed), afull (producer warps
+// wrote A), empty (MMAs that read the stage completed).  The producers then
+// read the MT accumulators back (tcgen05.ld) and store U directly.  Every wait
+// is bounded; on a timeout the CTA sets plan.status, drains its copies and
+// MMAs (bounded) and frees its tensor memory.
+#include "common.cuh"
+#include "tcgen05.cuh"
+
+namespace qsft {
+namespace gm {
+using namespace qsft::tc;
+
+constexpr int KC = 32;                     // K entries per stage (2 MMAs of K = 16)
+constexpr int TM = 128;                    // rows per MMA tile
+constexpr int HDR = 1024;                  // barriers, TMEM slot, flags, root table
+constexpr int MAX_STAGES = 4;
+constexpr int MAX_MT = 4;
+constexpr uint32_t SBO = KC * 16;          // bytes between 8-row core-matrix groups
+constexpr uint32_t A_TILE = TM * KC * 2;   // bytes of one tile's A chunk
+constexpr int PREP_S = 32;                 // support vectors per operand block
+constexpr int REGION_HDR = 256;            // per-job header (inverse scale)
+constexpr int MAX_SMEM = 227 * 1024;
+
+struct Geo {
+  int NP, S_pad, nK;
+  uint32_t CB;       // bytes of one B chunk (NP x KC FP16)
+  int64_t region_c;  // bytes per group: nK chunks + j table, 256-aligned
+};
+__host__ __device__ inline Geo geo(int RP, int S, int kps, int nw) {
+  Geo g;
+  g.NP = (2 * RP + 15) / 16 * 16;
+  const int spc = KC / kps;
+  g.S_pad = (S + spc - 1) / spc * spc;
+  g.nK = g.S_pad * kps / KC;
+  g.CB = (uint32_t)g.NP * KC * 2;
+  g.region_c = ((int64_t)g.nK * g.CB + (int64_t)g.S_pad * nw * 4 + 255) / 256 * 256;
+  return g;
+}
+__host__ __device__ inline int64_t region_bytes(const Geo& g, int C) { return REGION_HDR + (int64_t)C * g.region_c; }
+
+__host__ __device__ inline uint32_t stage_bytes(int mt, int npmax) { return (uint32_t)mt * A_TILE + (uint32_t)npmax * KC * 2; }
+
+// FP16 bits of x, and of the remainder x - hi
+__device__ __forceinline__ void split_h(double x, __half& hi, __half& lo) {
+  hi = __double2half(x);
+  lo = __double2half(x - (double)__half2float(hi));
+}
+__device__ __forceinline__ uint32_t h2_bits(__half lo16, __half hi16) {
+  const __half2 h = __halves2half2(lo16, hi16);
+  return *reinterpret_cast<const uint32_t*>(&h);
+}
+
+// ---------------------------------------------------------------- operands
+// Block = (job, group, 32 support vectors).  Writes the scaled C halves into
+// the B chunks and the packed j_s digits (digit t in byte t%4 of word t/4;
+// for q = 2 the digit is doubled so that the GEMM kernel works mod 4).
+template <int KPS, int NW>
+__global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
+  const int nj = plan.njobs;
+  const int64_t* __restrict__ idx = plan.gm_index;
+  const int64_t w = blockIdx.x;
+  const int j = find_job(idx + nj + 1, nj, w);
+  const qsft_job* __restrict__ job = plan.jobs + j;
+  const int q = job->q, n = job->n, b = job->b, S = job->S, RP = job->R * job->P;
+  const Geo g = geo(RP, S, KPS, NW);
+  const int sblocks = (g.S_pad + PREP_S - 1) / PREP_S;
+  const int64_t local = w - idx[nj + 1 + j];
+  const int c = (int)(local / sblocks);
+  const int sb = (int)(local - (int64_t)c * sblocks);
+  const int s_lo = sb * PREP_S, s_hi = min(s_lo + PREP_S, g.S_pad);
+  const float2* __restrict__ A = reinterpret_cast<const float2*>(plan.A) + job->off_A;
+  const int8_t* __restrict__ M = plan.i8 + job->off_M + (int64_t)c * n * b;
+  const int8_t* __restrict__ D = plan.i8 + job->off_D + (int64_t)c * RP * n;
+  const int8_t* __restrict__ K = plan.i8 + job->off_K;
+  unsigned char* region = reinterpret_cast<unsigned char*>(plan.gm_ws) + idx[2 * (nj + 1) + j];
+  unsigned char* rc = region + REGION_HDR + (int64_t)c * g.region_c;
+
+  // scale: 2^(14 - e) with max|a_s| < 2^e
+  __shared__ float red[8];
+  float mx = 0.f;
+  for (int s = threadIdx.x; s < S; s += blockDim.x) {
+    const float2 a = A[s];
+    mx = fmaxf(mx, sqrtf(a.x * a.x + a.y * a.y));
+  }
+  for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(~0u, mx, o));
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  mx = red[0];
+  for (int i = 1; i < (int)(blockDim.x >> 5); ++i) mx = fmaxf(mx, red[i]);
+  int ex = 0;
+  if (mx > 0.f && isfinite(mx)) frexpf(mx, &ex);
+  if (c == 0 && sb == 0 && threadIdx.x == 0) *reinterpret_cast<float*>(region) = ldexpf(1.0f, ex - 14);
+  const double sc = ldexp(1.0, 14 - ex);
+
+  // j table
+  uint32_t* jtab = reinterpret_cast<uint32_t*>(rc + (int64_t)g.nK * g.CB);
+  for (int e = threadIdx.x; e < (s_hi - s_lo) * NW; e += blockDim.x) {
+    const int s = s_lo + e / NW, wi = e % NW;
+    uint32_t word = 0;
+    if (s < S) {
+      for (int k = 0; k < 4; ++k) {
+        const int t = wi * 4 + k;
+        if (t >= b) break;
+        int acc = 0;
+        for (int i = 0; i < n; ++i) acc += (int)M[i * b + t] * (int)K[(int64_t)s * n + i];
+        uint32_t v = (uint32_t)(acc % q);
+        if (KPS == 4 && q == 2) v *= 2;
+        word |= v << (8 * k);
+      }
+    }
+    jtab[(int64_t)s * NW + wi] = word;
+  }
+
+  // B entries: one (support vector, column) per item
+  for (int e = threadIdx.x; e < (s_hi - s_lo) * g.NP; e += blockDim.x) {
+    const int s = s_lo + e / g.NP, nn = e % g.NP;
+    uint32_t v0 = 0, v1 = 0;  // the four FP16 entries of this column, as two half2 words
+    if (s < S && nn < 2 * RP) {
+      const int rp = nn >> 1;
+      int acc = 0;
+      for (int i = 0; i < n; ++i) acc += (int)D[rp * n + i] * (int)K[(int64_t)s * n + i];
+      const double2 wr = root_of_unity(acc % q, q);
+      const float2 a = A[s];
+      const double cr = ((double)a.x * wr.x - (double)a.y * wr.y) * sc;
+      const double ci = ((double)a.x * wr.y + (double)a.y * wr.x) * sc;
+      __half hr, lr, hi, li;
+      split_h(cr, hr, lr);
+      split_h(ci, hi, li);
+      if ((nn & 1) == 0) {
+        v0 = h2_bits(hr, __hneg(hi));
+        v1 = h2_bits(lr, __hneg(li));
+      } else {
+        v0 = h2_bits(hi, hr);
+        v1 = h2_bits(li, lr);
+      }
+    }
+    const int k0 = KPS * s;
+    const int kc = k0 / KC, kin = k0 % KC;
+    unsigned char* dst = rc + (int64_t)kc * g.CB + (nn >> 3) * (KC * 16) + (kin >> 3) * 128 + (nn & 7) * 16 +
+                         (kin & 7) * 2;
+    if (KPS == 4)
+      *reinterpret_cast<uint2*>(dst) = make_uint2(v0, v1);
+    else
+      *reinterpret_cast<uint4*>(dst) = make_uint4(v0, v1, v0, v1);
+  }
+}
+
+// ---------------------------------------------------------------- GEMM
+template <int KPS, int NW>
+__global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_plan plan, int ns) {
+  extern __shared__ __align__(1024) unsigned char smem[];
+  uint64_t* bfull = reinterpret_cast<uint64_t*>(smem);  // [MAX_STAGES]
+  uint64_t* afull = bfull + MAX_STAGES;
+  uint64_t* empty = afull + MAX_STAGES;
+  uint64_t* accf = empty + MAX_STAGES;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 256);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 260);
+  volatile int* n_con = reinterpret_cast<volatile int*>(smem + 264);
+  uint2* qtab = reinterpret_cast<uint2*>(smem + 512);  // KPS = 8: (hi, lo) half2 words of omega^m
+  uint32_t* jt = reinterpret_cast<uint32_t*>(smem + HDR);
+  unsigned char* stage0 = smem + HDR + plan.gm_jt_bytes;
+  const int MT = plan.gm_mt;
+  const uint32_t A_BYTES = (uint32_t)MT * A_TILE;
+  const uint32_t STAGE = stage_bytes(MT, plan.gm_npmax);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int nprod = MT * TM;
+  const int mma_warp = nprod / 32, load_warp = mma_warp + 1;
+
+  // ---- work item: (job, group, block of MT*128 rows)
+  const int nj = plan.njobs;
+  const int64_t* __restrict__ idx = plan.gm_index;
+  const int64_t w = blockIdx.x;
+  const int j = find_job(idx, nj, w);
+  const qsft_job* __restrict__ job = plan.jobs + j;
+  const int q = job->q, b = job->b, B = job->B, S = job->S, RP = job->R * job->P;
+  const Geo g = geo(RP, S, KPS, NW);
+  const int64_t rblocks = (B + nprod - 1) / nprod;
+  const int64_t local = w - idx[j];
+  const int c = (int)(local / rblocks);
+  const int64_t row0 = (local - (int64_t)c * rblocks) * nprod;
+  const unsigned char* region = reinterpret_cast<const unsigned char*>(plan.gm_ws) + idx[2 * (nj + 1) + j];
+  const unsigned char* gB = region + REGION_HDR + (int64_t)c * g.region_c;
+  const uint32_t* gJ = reinterpret_cast<const uint32_t*>(gB + (int64_t)g.nK * g.CB);
+  float2* __restrict__ U = reinterpret_cast<float2*>(plan.U) + job->off_U + (int64_t)c * RP * B;
+
+  // ---- setup
+  uint32_t ncols = 32;
+  while (ncols < (uint32_t)(MT * g.NP)) ncols <<= 1;
+  if (warp == mma_warp) {
+    tmem_alloc(tmem_slot, ncols);
+    tmem_relinquish();
+  }
+  if (tid == 0) {
+    for (int i = 0; i < MAX_STAGES; ++i) {
+      mbar_init(&bfull[i], 1);
+      mbar_init(&afull[i], MT * 4);
+      mbar_init(&empty[i], 1);
+    }
+    mbar_init(accf, 1);
+    *abort_flag = 0;
+    *n_con = 0;
+    fence_mbar_init();
+  }
+  if (KPS == 8 && tid < q) {
+    const double2 wr = root_of_unity(tid, q);
+    __half hr, lr, hi, li;
+    split_h(wr.x, hr, lr);
+    split_h(wr.y, hi, li);
+    qtab[tid] = make_uint2(h2_bits(hr, hi), h2_bits(lr, li));
+  }
+  for (int i = tid; i < g.S_pad * NW; i += blockDim.x) jt[i] = __ldg(gJ + i);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const int nK = g.nK;
+  int iss = 0;  // bulk copies issued (load warp, lane 0)
+
+  if (tid < nprod) {
+    // ---- producers: one row of A per thread
+    const int t = tid >> 7, tr = tid & (TM - 1);
+    const int64_t l = row0 + tid;
+    uint32_t lw[NW];
+#pragma unroll
+    for (int k = 0; k < NW; ++k) lw[k] = 0;
+    if (l < B) {
+      uint32_t v = (uint32_t)l;
+#pragma unroll
+      for (int d = 4 * NW - 1; d >= 0; --d) {  // MSB-first digits: digit b-1 is l mod q
+        if (d < b) {
+          const uint32_t qt = v / (uint32_t)q;
+          lw[d >> 2] |= (v - qt * (uint32_t)q) << (8 * (d & 3));
+          v = qt;
+        }
+      }
+    }
+    const ModQ mq = make_modq(q);
+    const uint32_t a_off = (uint32_t)t * A_TILE + (tr >> 3) * SBO + (tr & 7) * 16;
+    for (int kc = 0; kc < nK; ++kc) {
+      const int st = kc % ns;
+      const uint32_t ph = (uint32_t)(kc / ns) & 1;
+      int go = 1;
+      if (lane == 0) go = !*abort_flag && mbar_wait(&empty[st], ph ^ 1);
+      go = __shfl_sync(~0u, go, 0);
+      if (!go) {
+        if (lane == 0) *abort_flag = 1;
+        break;
+      }
+      unsigned char* ap = stage0 + st * STAGE + a_off;
+      const int s0 = kc * (KC / KPS);
+      if constexpr (KPS == 4) {
+        // omega_4^m as half2 (re, im): high bytes from the tables 0x00BC003C (re)
+        // and 0xBC003C00 (im), low bytes zero
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const uint32_t* jp = jt + (s0 + 2 * i) * NW;
+          uint32_t d0 = 0, d1 = 0;
+#pragma unroll
+          for (int k = 0; k < NW; ++k) {
+            d0 = __dp4a(lw[k], jp[k], d0);
+            d1 = __dp4a(lw[k], jp[NW + k], d1);
+          }
+          const uint32_t w0 = __byte_perm(0x00BC003Cu, 0xBC003C00u, 0x4101u + (d0 & 3u) * 0x1010u);
+          const uint32_t w1 = __byte_perm(0x00BC003Cu, 0xBC003C00u, 0x4101u + (d1 & 3u) * 0x1010u);
+          *reinterpret_cast<uint4*>(ap + i * 128) = make_uint4(w0, w0, w1, w1);
+        }
+      } else {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const uint32_t* jp = jt + (s0 + i) * NW;
+          uint32_t d = 0;
+#pragma unroll
+          for (int k = 0; k < NW; ++k) d = __dp4a(lw[k], jp[k], d);
+          const uint2 h = qtab[modq(d, mq)];
+          *reinterpret_cast<uint4*>(ap + i * 128) = make_uint4(h.x, h.x, h.y, h.y);
+        }
+      }
+      fence_async_smem();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&afull[st]);
+    }
+    // ---- epilogue: accumulators -> U
+    int ok = 1;
+    if (lane == 0) ok = mbar_wait(accf, 0) && !*abort_flag;
+    ok = __shfl_sync(~0u, ok, 0);
+    tc_fence_after();
+    if (ok) {
+      const int lq = warp & 3;
+      const int64_t row = row0 + t * TM + lq * 32 + lane;
+      const bool live = row < B;
+      const uint32_t tb = tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(t * g.NP);
+      float2* __restrict__ ur = U + row;
+      const float inv = *reinterpret_cast<const float*>(region);
+      const int ng = g.NP / 16;
+      uint32_t ra[16], rb[16];
+      tmem_ld16(tb, ra);
+      for (int cg = 0; cg < ng; cg += 2) {
+        tmem_ld_wait_regs(ra);
+        if (cg + 1 < ng) tmem_ld16(tb + (cg + 1) * 16, rb);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int rp = cg * 8 + i;
+          if (live && rp < RP)
+            ur[(int64_t)rp * B] = make_float2(__uint_as_float(ra[2 * i]) * inv, __uint_as_float(ra[2 * i + 1]) * inv);
+        }
+        if (cg + 1 < ng) {
+          tmem_ld_wait_regs(rb);
+          if (cg + 2 < ng) tmem_ld16(tb + (cg + 2) * 16, ra);
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const int rp = (cg + 1) * 8 + i;
+            if (live && rp < RP)
+              ur[(int64_t)rp * B] =
+                  make_float2(__uint_as_float(rb[2 * i]) * inv, __uint_as_float(rb[2 * i + 1]) * inv);
+          }
+        }
+      }
+    } else if (lane == 0) {
+      *abort_flag = 1;
+    }
+  } else if (warp == mma_warp) {
+    // ---- MMA issue
+    if (lane == 0) {
+      const uint32_t idesc = tc::make_idesc(TM, g.NP);
+      int con = 0;
+      for (int kc = 0; kc < nK; ++kc) {
+        const int st = kc % ns;
+        const uint32_t ph = (uint32_t)(kc / ns) & 1;
+        if (*abort_flag) break;
+        if (!mbar_wait(&bfull[st], ph) || !mbar_wait(&afull[st], ph)) {
+          *abort_flag = 1;
+          break;
+        }
+        tc_fence_after();
+        const uint32_t a_base = smem_u32(stage0 + st * STAGE), b_base = a_base + A_BYTES;
+        for (int t = 0; t < MT; ++t) {
+#pragma unroll
+          for (int ks = 0; ks < KC / 16; ++ks)
+            mma_f16(tmem + (uint32_t)(t * g.NP), make_desc(a_base + t * A_TILE + ks * 256, 128, SBO),
+                    make_desc(b_base + ks * 256, 128, SBO), idesc, (kc | ks) > 0);
+        }
+        mma_commit(&empty[st]);
+        con = kc + 1;
+      }
+      mma_commit(accf);  // arrives once every MMA issued above has completed
+      *n_con = con;
+    }
+    __syncwarp();
+  } else if (warp == load_warp) {
+    // ---- B chunks: one bulk copy per stage
+    if (lane == 0) {
+      for (int kc = 0; kc < nK; ++kc) {
+        const int st = kc % ns;
+        const uint32_t ph = (uint32_t)(kc / ns) & 1;
+        if (*abort_flag) break;
+        if (!mbar_wait(&empty[st], ph ^ 1)) {
+          *abort_flag = 1;
+          break;
+        }
+        mbar_arrive_expect_tx(&bfull[st], g.CB);
+        bulk_g2s(stage0 + st * STAGE + A_BYTES, gB + (int64_t)kc * g.CB, g.CB, &bfull[st]);
+        iss = kc + 1;
+      }
+    }
+    __syncwarp();
+  }
+  __syncthreads();  // every role loop has ended; n_con is final
+  if (warp == load_warp && lane == 0)
+    for (int kc = *n_con; kc < iss; ++kc)  // copies that no MMA consumed: let them land (bounded)
+      mbar_wait(&bfull[kc % ns], (uint32_t)(kc / ns) & 1);
+  if (warp == mma_warp && lane == 0 && *abort_flag) mbar_wait(accf, 0);  // MMAs done before dealloc
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (tid == 0 && *abort_flag) atomicExch(plan.status, (int)QSFT_ERR_TIMEOUT);
+  if (warp == mma_warp) tmem_dealloc(tmem, ncols);
+}
+
+template <int KPS, int NW>
+static int launch(const qsft_plan* p, cudaStream_t st) {
+  const uint32_t stage = stage_bytes(p->gm_mt, p->gm_npmax);
+  const int fixed = HDR + p->gm_jt_bytes;
+  int ns = (MAX_SMEM - fixed) / (int)stage;
+  if (ns > MAX_STAGES) ns = MAX_STAGES;
+  if (ns < 2) return QSFT_ERR_TOO_LARGE;
+  const int smem = fixed + ns * (int)stage;
+  if (p->total_gm_prep > 0) {
+    gemm_prep_kernel<KPS, NW><<<(unsigned)p->total_gm_prep, 256, 0, st>>>(*p);
+    QSFT_CUDA_CHECK_LAUNCH();
+  }
+  auto kern = eval_gemm_kernel<KPS, NW>;
+  if (!ensure_smem((const void*)kern, smem)) return QSFT_ERR_CUDA;
+  kern<<<(unsigned)p->total_gm_work, p->gm_mt * TM + 64, smem, st>>>(*p, ns);
+  QSFT_CUDA_CHECK_LAUNCH();
+  return QSFT_OK;
+}
+
+template <int KPS>
+static int launch_nw(const qsft_plan* p, cudaStream_t st) {
+  switch (p->gm_nw) {
+    case 1: return launch<KPS, 1>(p, st);
+    case 2: return launch<KPS, 2>(p, st);
+    case 4: return launch<KPS, 4>(p, st);
+    default: return QSFT_ERR_ARG;
+  }
+}
+
+}  // namespace gm
+}  // namespace qsft
+
+using namespace qsft;
+
+extern "C" int qsft_gemm_layout(const qsft_job* jobs, int njobs, qsft_plan* plan, int64_t* index) {
+  if (!jobs || njobs <= 0 || !plan || !index) return QSFT_ERR_ARG;
+  int kps = 4, maxb = 0, npmax = 16, jt = 0;
+  int64_t maxB = 1;
+  for (int i = 0; i < njobs; ++i) {
+    const qsft_job& jb = jobs[i];
+    if (jb.q < 2 || jb.n < 1 || jb.b < 1 || jb.C < 1 || jb.R < 1 || jb.P < 1 || jb.S < 1) return QSFT_ERR_ARG;
+    if (jb.q > QSFT_MAX_Q || jb.b > 16 || 2 * jb.R * jb.P > 256 || jb.S > 8192 || jb.n > QSFT_MAX_N)
+      return QSFT_ERR_TOO_LARGE;
+    if (jb.q != 2 && jb.q != 4) kps = 8;
+    maxb = maxb > jb.b ? maxb : jb.b;
+    maxB = maxB > jb.B ? maxB : jb.B;
+    const int np = (2 * jb.R * jb.P + 15) / 16 * 16;
+    npmax = npmax > np ? npmax : np;
+  }
+  const int nw = maxb <= 4 ? 1 : (maxb <= 8 ? 2 : 4);
+  int mt = gm::MAX_MT;
+  while (mt > 1 && (mt * npmax > 512 || (int64_t)(mt / 2) * gm::TM >= maxB)) mt /= 2;
+  int64_t work = 0, prep = 0, off = 0;
+  index[0] = 0;
+  index[njobs + 1] = 0;
+  for (int i = 0; i < njobs; ++i) {
+    const qsft_job& jb = jobs[i];
+    const gm::Geo g = gm::geo(jb.R * jb.P, jb.S, kps, nw);
+    const int64_t rows = (int64_t)mt * gm::TM;
+    work += (int64_t)jb.C * ((jb.B + rows - 1) / rows);
+    prep += (int64_t)jb.C * ((g.S_pad + gm::PREP_S - 1) / gm::PREP_S);
+    index[i + 1] = work;
+    index[njobs + 2 + i] = prep;
+    index[2 * (njobs + 1) + i] = off;
+    off += gm::region_bytes(g, jb.C);
+    const int jtb = (g.S_pad * nw * 4 + 127) / 128 * 128;
+    jt = jt > jtb ? jt : jtb;
+  }
+  if (gm::HDR + jt + 2 * (int)gm::stage_bytes(mt, npmax) > gm::MAX_SMEM) return QSFT_ERR_TOO_LARGE;
+  if (work > 0x7fffffffLL || prep > 0x7fffffffLL) return QSFT_ERR_TOO_LARGE;
+  plan->gm_mt = mt;
+  plan->gm_kps = kps;
+  plan->gm_nw = nw;
+  plan->gm_npmax = npmax;
+  plan->gm_jt_bytes = jt;
+  plan->total_gm_work = work;
+  plan->total_gm_prep = prep;
+  plan->gm_ws_bytes = off;
+  return QSFT_OK;
+}
+
+extern "C" int qsft_eval_cosets_gemm(const qsft_plan* plan, qsft_stream_t stream) {
+  if (!plan || plan->njobs <= 0 || !plan->jobs || !plan->gm_index || !plan->gm_ws || !plan->i8 || !plan->A ||
+      !plan->U || !plan->status)
+    return QSFT_ERR_ARG;
+  if (plan->prec != QSFT_F32) return QSFT_ERR_ARG;
+  if (plan->gm_mt != 1 && plan->gm_mt != 2 && plan->gm_mt != 4) return QSFT_ERR_ARG;
+  if (plan->gm_npmax < 16 || plan->gm_npmax > 256 || plan->gm_npmax % 16 || plan->gm_mt * plan->gm_npmax > 512)
+    return QSFT_ERR_ARG;
+  if (plan->total_gm_work <= 0) return QSFT_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (plan->gm_kps == 4) {
+    if (plan->max_q > 4) return QSFT_ERR_ARG;
+    return gm::launch_nw<4>(plan, st);
+  }
+  if (plan->gm_kps == 8) return gm::launch_nw<8>(plan, st);
+  return QSFT_ERR_ARG;
+}

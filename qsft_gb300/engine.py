@@ -269,6 +269,14 @@ class Batch:
         p.tc_smax, p.tc_npad, p.tc_table_bytes = self.tc_smax, self.tc_npad, self.tc_table_bytes
         p.tc_entry_bytes = self.tc_entry_bytes
         p.status = ptr(self.status)
+        # coset-factored GEMM evaluation (FP32): operand workspace and work index
+        index = (ctypes.c_int64 * (3 * J + 2))()
+        self.gm_ok = (self.prec == QSFT_F32 and
+                      self.lib.qsft_gemm_layout(self.jobs_host, J, ctypes.byref(p), index) == 0)
+        if self.gm_ok:
+            self.gm_ws = torch.empty(max(int(p.gm_ws_bytes), 256), dtype=torch.uint8, device=dev)
+            self.gm_index = up(np.frombuffer(index, dtype=np.int64).copy(), torch.int64)
+            p.gm_ws, p.gm_index = ptr(self.gm_ws), ptr(self.gm_index)
         self.plan = p
 
     # ------------------------------------------------------------ inputs
@@ -312,14 +320,28 @@ class Batch:
         n_el = sp.C * sp.R * sp.P * sp.B
         return self.U[jb.off_U:jb.off_U + n_el].view(sp.C, sp.R * sp.P, sp.B)
 
-    def eval(self, stream=None, tensor_cores=None):
-        """Coset evaluation; FP32 batches use the tensor-core kernel unless tensor_cores=False."""
-        use_tc = (self.prec == QSFT_F32 and self.tc_ok) if tensor_cores is None else bool(tensor_cores)
-        if use_tc:
+    def eval_method(self):
+        """The evaluation kernel ``eval`` picks: "gemm" (coset-factored tensor-core
+        GEMM), "tc" (tensor-core dot products + CUDA-core reduction) or "cuda"."""
+        if self.prec != QSFT_F32:
+            return "cuda"
+        return "gemm" if self.gm_ok else ("tc" if self.tc_ok else "cuda")
+
+    def eval(self, stream=None, method=None):
+        """Coset evaluation into U with `method` (default: ``eval_method()``)."""
+        method = method or self.eval_method()
+        if method == "gemm":
+            if not self.gm_ok:
+                raise ValueError("this batch is outside the GEMM evaluation's limits")
+            check(self.lib.qsft_eval_cosets_gemm(ctypes.byref(self.plan), stream_handle(stream)),
+                  "qsft_eval_cosets_gemm")
+        elif method == "tc":
             self.U.zero_()   # the tensor-core kernel accumulates partial sums into U
             check(self.lib.qsft_eval_cosets_tc(ctypes.byref(self.plan), stream_handle(stream)), "qsft_eval_cosets_tc")
-        else:
+        elif method == "cuda":
             check(self.lib.qsft_eval_cosets(ctypes.byref(self.plan), stream_handle(stream)), "qsft_eval_cosets")
+        else:
+            raise ValueError(f"unknown evaluation method {method!r}")
 
     def gwht(self, stream=None):
         for (q, b), rows in self.gwht_groups.items():

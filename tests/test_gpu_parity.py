@@ -232,19 +232,24 @@ def _random_spec(rng, q, n, b, S, C, R, chan="nso"):
     [(20, 10, 3, 1500, 2, 1)],                     # support split over several chunks
     [(4, 12, 5, 60, 3, 2), (3, 9, 4, 20, 3, 1), (20, 6, 2, 30, 3, 3), (2, 16, 8, 40, 3, 2)],  # mixed batch
 ])
-def test_eval_tensor_cores_vs_cuda_cores_and_oracle(cuda, shapes):
-    """tcgen05 coset evaluation == CUDA-core evaluation == oracle (FP32 tolerance)."""
+@pytest.mark.parametrize("method", ["gemm", "tc"])
+def test_eval_tensor_cores_vs_cuda_cores_and_oracle(cuda, shapes, method):
+    """tcgen05 coset evaluation (coset-factored GEMM, or dot products + lookup)
+    == CUDA-core evaluation == oracle (FP32 tolerance)."""
     from qsft_gb300.engine import Batch
     rng = np.random.RandomState(len(shapes) * 7 + shapes[0][0])
     specs = [_random_spec(rng, *sh) for sh in shapes]
     bt = Batch(specs, precision="fp32")
-    bt.eval(tensor_cores=True)
+    assert bt.gm_ok
+    bt.U.fill_(float("nan"))     # every sample must be written
+    bt.eval(method=method)
     tc = [bt.job_U(j).cpu().numpy().copy() for j in range(len(specs))]
     assert bt.device_status() == 0
-    bt.eval(tensor_cores=False)
+    bt.eval(method="cuda")
     cc = [bt.job_U(j).cpu().numpy().copy() for j in range(len(specs))]
     for sp, a, c in zip(specs, tc, cc):
         scale = np.abs(c).max()
+        assert np.all(np.isfinite(a))
         assert np.max(np.abs(a - c)) / scale < 2e-6 * np.sqrt(sp.S)
         # oracle on one coset row of each group
         for g in range(sp.C):
