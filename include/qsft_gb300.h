@@ -227,7 +227,8 @@ int qsft_eval_cosets_gemm(const qsft_plan* plan, qsft_stream_t stream);
  * Host-side sizing for qsft_eval_cosets_gemm: from the jobs' shapes (q, n, b,
  * C, R, P, S, B), fills plan->gm_mt, gm_kps, gm_nw, gm_npmax, gm_jt_bytes,
  * total_gm_work, total_gm_prep, gm_ws_bytes and index_host[3*njobs+2] (to be
- * uploaded to plan->gm_index).  QSFT_ERR_TOO_LARGE when a job is outside the
+ * uploaded to plan->gm_index).  A plan->gm_mt of 1 or 2 on entry caps the
+ * 128-row tiles per CTA (default 4).  QSFT_ERR_TOO_LARGE when a job is outside the
  * kernel's limits (q > 32, b > 16, 2*R*P > 256, S > 8192): use
  * qsft_eval_cosets_tc for such batches.
  */

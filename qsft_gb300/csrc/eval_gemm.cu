@@ -26,18 +26,19 @@
 //     B rows repeat the four KPS = 4 rows twice.
 // N = 2*R*P rounded up to 16 (<= 256).  An operand kernel writes B (and the
 // packed j_s digits) into a workspace in the exact shared-memory image of each
-// 32-entry K chunk, so the GEMM kernel streams it with one bulk copy per
+// 64-entry K chunk (128-byte-swizzled K-major rows), so the GEMM kernel streams it with one bulk copy per
 // stage.  The GEMM kernel generates A in shared memory from the row's digits
 // (two dp4a per support vector for b <= 8) and issues tcgen05.mma kind::f16
 // (M = 128, N, K = 16) into tensor memory.
 //
 // CTA: MT tiles of 128 rows (one producer thread per row, MT*128 threads),
-// one MMA-issuing warp and one bulk-copy warp.  Stages of (A, B) chunks in a
-// ring guarded by mbarriers: bfull (bulk copy landed), afull (producer warps
-// wrote A), empty (MMAs that read the stage completed).  The producers then
-// read the MT accumulators back (tcgen05.ld) and store U directly.  Every wait
-// is bounded; on a timeout the CTA sets plan.status, drains its copies and
-// MMAs (bounded) and frees its tensor memory.
+// one MMA-issuing warp and one bulk-copy warp.  A chunks and B chunks live in
+// two rings of their own (B deeper: its copies come from L2), each guarded by
+// mbarriers: afull (producer warps wrote A) / aempty (the MMAs that read it
+// completed), bfull (bulk copy landed) / bempty.  The producers then read the
+// MT accumulators back (tcgen05.ld) and store U directly.  Every wait is
+// bounded; on a timeout the CTA sets plan.status, drains its copies and MMAs
+// (bounded) and frees its tensor memory.
 #include "common.cuh"
 #include "tcgen05.cuh"
 
@@ -45,13 +46,11 @@ namespace qsft {
 namespace gm {
 using namespace qsft::tc;
 
-constexpr int KC = 32;                     // K entries per stage (2 MMAs of K = 16)
+constexpr int KC = 64;                     // K entries per stage: one 128-byte row (4 MMAs of K = 16)
 constexpr int TM = 128;                    // rows per MMA tile
 constexpr int HDR = 1024;                  // barriers, TMEM slot, flags, root table
-constexpr int MAX_STAGES = 4;
 constexpr int MAX_MT = 4;
-constexpr uint32_t SBO = KC * 16;          // bytes between 8-row core-matrix groups
-constexpr uint32_t A_TILE = TM * KC * 2;   // bytes of one tile's A chunk
+constexpr uint32_t A_TILE = TM * KC * 2;   // bytes of one tile's A chunk (16 KB)
 constexpr int PREP_S = 32;                 // support vectors per operand block
 constexpr int REGION_HDR = 256;            // per-job header (inverse scale)
 constexpr int MAX_SMEM = 227 * 1024;
@@ -73,7 +72,20 @@ __host__ __device__ inline Geo geo(int RP, int S, int kps, int nw) {
 }
 __host__ __device__ inline int64_t region_bytes(const Geo& g, int C) { return REGION_HDR + (int64_t)C * g.region_c; }
 
-__host__ __device__ inline uint32_t stage_bytes(int mt, int npmax) { return (uint32_t)mt * A_TILE + (uint32_t)npmax * KC * 2; }
+// Operand tiles use the 128-byte-swizzled K-major layout: a row of a tile is
+// its 64 K entries (128 bytes), 8 rows form a 1024-byte atom, and the 16-byte
+// chunk c of row r is stored at chunk c ^ (r % 8).  Offset of entry k of row r:
+__host__ __device__ inline uint32_t sw128(int r, int k) {
+  return (uint32_t)(r >> 3) * 1024 + (uint32_t)(r & 7) * 128 + (uint32_t)(((k >> 3) ^ (r & 7)) * 16) +
+         (uint32_t)(k & 7) * 2;
+}
+// tcgen05 shared-memory descriptor of such a tile (atoms 1024-byte aligned):
+// start >> 4, LBO 16 B (unused for swizzled K-major), SBO 1024 B between 8-row
+// groups, version 1, layout type 2 = 128-byte swizzle
+__device__ __forceinline__ uint64_t desc_sw128(uint32_t saddr) {
+  return (uint64_t)((saddr >> 4) & 0x3FFFu) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
 
 // FP16 bits of x, and of the remainder x - hi
 __device__ __forceinline__ void split_h(double x, __half& hi, __half& lo) {
@@ -89,8 +101,17 @@ __device__ __forceinline__ uint32_t h2_bits(__half lo16, __half hi16) {
 // Block = (job, group, 32 support vectors).  Writes the scaled C halves into
 // the B chunks and the packed j_s digits (digit t in byte t%4 of word t/4;
 // for q = 2 the digit is doubled so that the GEMM kernel works mod 4).
+// FP32 throughout (GB300's FP64 rate is a small fraction of FP32): a_s is
+// FP32 already, the roots come from plan.roots, and the power-of-two scaling
+// is exact, so hi + lo carry C to FP32 accuracy.
+constexpr int PREP_MAXN = QSFT_MAX_N;
+constexpr int PREP_MAXRP = 128;
 template <int KPS, int NW>
 __global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
+  __shared__ int8_t sK[PREP_S * PREP_MAXN];
+  __shared__ int8_t sD[PREP_MAXRP * PREP_MAXN];
+  __shared__ float2 sW[QSFT_MAX_Q];
+  __shared__ float red[8];
   const int nj = plan.njobs;
   const int64_t* __restrict__ idx = plan.gm_index;
   const int64_t w = blockIdx.x;
@@ -102,101 +123,116 @@ __global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
   const int64_t local = w - idx[nj + 1 + j];
   const int c = (int)(local / sblocks);
   const int sb = (int)(local - (int64_t)c * sblocks);
-  const int s_lo = sb * PREP_S, s_hi = min(s_lo + PREP_S, g.S_pad);
+  const int s_lo = sb * PREP_S, s_hi = min(s_lo + PREP_S, g.S_pad), s_live = max(0, min(s_hi, S) - s_lo);
   const float2* __restrict__ A = reinterpret_cast<const float2*>(plan.A) + job->off_A;
   const int8_t* __restrict__ M = plan.i8 + job->off_M + (int64_t)c * n * b;
   const int8_t* __restrict__ D = plan.i8 + job->off_D + (int64_t)c * RP * n;
-  const int8_t* __restrict__ K = plan.i8 + job->off_K;
+  const int8_t* __restrict__ K = plan.i8 + job->off_K + (int64_t)s_lo * n;
   unsigned char* region = reinterpret_cast<unsigned char*>(plan.gm_ws) + idx[2 * (nj + 1) + j];
   unsigned char* rc = region + REGION_HDR + (int64_t)c * g.region_c;
+  const int tid = threadIdx.x;
 
+  for (int i = tid; i < s_live * n; i += blockDim.x) sK[i] = K[i];
+  for (int i = tid; i < RP * n; i += blockDim.x) sD[i] = D[i];
+  if (tid < q) {
+    const double* r = plan.roots + ((int64_t)q * 32 + tid) * 2;
+    sW[tid] = make_float2((float)r[0], (float)r[1]);
+  }
   // scale: 2^(14 - e) with max|a_s| < 2^e
-  __shared__ float red[8];
   float mx = 0.f;
-  for (int s = threadIdx.x; s < S; s += blockDim.x) {
+  for (int s = tid; s < S; s += blockDim.x) {
     const float2 a = A[s];
     mx = fmaxf(mx, sqrtf(a.x * a.x + a.y * a.y));
   }
   for (int o = 16; o; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(~0u, mx, o));
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = mx;
+  if ((tid & 31) == 0) red[tid >> 5] = mx;
   __syncthreads();
   mx = red[0];
   for (int i = 1; i < (int)(blockDim.x >> 5); ++i) mx = fmaxf(mx, red[i]);
   int ex = 0;
   if (mx > 0.f && isfinite(mx)) frexpf(mx, &ex);
-  if (c == 0 && sb == 0 && threadIdx.x == 0) *reinterpret_cast<float*>(region) = ldexpf(1.0f, ex - 14);
-  const double sc = ldexp(1.0, 14 - ex);
+  if (c == 0 && sb == 0 && tid == 0) *reinterpret_cast<float*>(region) = ldexpf(1.0f, ex - 14);
+  const float sc = ldexpf(1.0f, 14 - ex);
 
   // j table
   uint32_t* jtab = reinterpret_cast<uint32_t*>(rc + (int64_t)g.nK * g.CB);
-  for (int e = threadIdx.x; e < (s_hi - s_lo) * NW; e += blockDim.x) {
-    const int s = s_lo + e / NW, wi = e % NW;
+  for (int e = tid; e < (s_hi - s_lo) * NW; e += blockDim.x) {
+    const int sl = e / NW, wi = e % NW;
     uint32_t word = 0;
-    if (s < S) {
+    if (sl < s_live) {
       for (int k = 0; k < 4; ++k) {
         const int t = wi * 4 + k;
         if (t >= b) break;
         int acc = 0;
-        for (int i = 0; i < n; ++i) acc += (int)M[i * b + t] * (int)K[(int64_t)s * n + i];
+        for (int i = 0; i < n; ++i) acc += (int)M[i * b + t] * (int)sK[sl * n + i];
         uint32_t v = (uint32_t)(acc % q);
         if (KPS == 4 && q == 2) v *= 2;
         word |= v << (8 * k);
       }
     }
-    jtab[(int64_t)s * NW + wi] = word;
+    jtab[(int64_t)(s_lo + sl) * NW + wi] = word;
   }
 
-  // B entries: one (support vector, column) per item
-  for (int e = threadIdx.x; e < (s_hi - s_lo) * g.NP; e += blockDim.x) {
-    const int s = s_lo + e / g.NP, nn = e % g.NP;
-    uint32_t v0 = 0, v1 = 0;  // the four FP16 entries of this column, as two half2 words
-    if (s < S && nn < 2 * RP) {
-      const int rp = nn >> 1;
-      int acc = 0;
-      for (int i = 0; i < n; ++i) acc += (int)D[rp * n + i] * (int)K[(int64_t)s * n + i];
-      const double2 wr = root_of_unity(acc % q, q);
-      const float2 a = A[s];
-      const double cr = ((double)a.x * wr.x - (double)a.y * wr.y) * sc;
-      const double ci = ((double)a.x * wr.y + (double)a.y * wr.x) * sc;
-      __half hr, lr, hi, li;
-      split_h(cr, hr, lr);
-      split_h(ci, hi, li);
-      if ((nn & 1) == 0) {
-        v0 = h2_bits(hr, __hneg(hi));
-        v1 = h2_bits(lr, __hneg(li));
-      } else {
-        v0 = h2_bits(hi, hr);
-        v1 = h2_bits(li, lr);
-      }
-    }
+  // B entries: (support vector, delay row) items write the row's two columns
+  auto dst = [&](int s, int nn) {
     const int k0 = KPS * s;
     const int kc = k0 / KC, kin = k0 % KC;
-    unsigned char* dst = rc + (int64_t)kc * g.CB + (nn >> 3) * (KC * 16) + (kin >> 3) * 128 + (nn & 7) * 16 +
-                         (kin & 7) * 2;
+    return rc + (int64_t)kc * g.CB + sw128(nn, kin);
+  };
+  auto put = [&](unsigned char* p, uint32_t v0, uint32_t v1) {
     if (KPS == 4)
-      *reinterpret_cast<uint2*>(dst) = make_uint2(v0, v1);
+      *reinterpret_cast<uint2*>(p) = make_uint2(v0, v1);
     else
-      *reinterpret_cast<uint4*>(dst) = make_uint4(v0, v1, v0, v1);
+      *reinterpret_cast<uint4*>(p) = make_uint4(v0, v1, v0, v1);
+  };
+  for (int e = tid; e < (s_hi - s_lo) * RP; e += blockDim.x) {
+    const int sl = e / RP, rp = e % RP, s = s_lo + sl;
+    uint32_t re0 = 0, re1 = 0, im0 = 0, im1 = 0;
+    if (sl < s_live) {
+      int acc = 0;
+      for (int i = 0; i < n; ++i) acc += (int)sD[rp * n + i] * (int)sK[sl * n + i];
+      const float2 wr = sW[acc % q];
+      const float2 a = A[s];
+      const float cr = (a.x * wr.x - a.y * wr.y) * sc;
+      const float ci = (a.x * wr.y + a.y * wr.x) * sc;
+      const __half hr = __float2half_rn(cr), hi = __float2half_rn(ci);
+      const __half lr = __float2half_rn(cr - __half2float(hr)), li = __float2half_rn(ci - __half2float(hi));
+      re0 = h2_bits(hr, __hneg(hi));  // real-part column: [Chr, -Chi, Clr, -Cli]
+      re1 = h2_bits(lr, __hneg(li));
+      im0 = h2_bits(hi, hr);          // imaginary-part column: [Chi, Chr, Cli, Clr]
+      im1 = h2_bits(li, lr);
+    }
+    put(dst(s, 2 * rp), re0, re1);
+    put(dst(s, 2 * rp + 1), im0, im1);
+  }
+  for (int e = tid; e < (s_hi - s_lo) * (g.NP - 2 * RP); e += blockDim.x) {  // padding columns
+    const int sl = e / (g.NP - 2 * RP), nn = 2 * RP + e % (g.NP - 2 * RP);
+    put(dst(s_lo + sl, nn), 0u, 0u);
   }
 }
 
 // ---------------------------------------------------------------- GEMM
+constexpr int MAX_NA = 4;  // A stages
+constexpr int MAX_NB = 8;  // B stages (deeper: their bulk copies come from L2)
+
 template <int KPS, int NW>
-__global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_plan plan, int ns) {
+__global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_plan plan, int na, int nb) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  uint64_t* bfull = reinterpret_cast<uint64_t*>(smem);  // [MAX_STAGES]
-  uint64_t* afull = bfull + MAX_STAGES;
-  uint64_t* empty = afull + MAX_STAGES;
-  uint64_t* accf = empty + MAX_STAGES;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 256);
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 260);
-  volatile int* n_con = reinterpret_cast<volatile int*>(smem + 264);
+  uint64_t* bfull = reinterpret_cast<uint64_t*>(smem);  // [MAX_NB]
+  uint64_t* bempty = bfull + MAX_NB;                    // [MAX_NB]
+  uint64_t* afull = bempty + MAX_NB;                    // [MAX_NA]
+  uint64_t* aempty = afull + MAX_NA;                    // [MAX_NA]
+  uint64_t* accf = aempty + MAX_NA;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 384);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 388);
+  volatile int* n_con = reinterpret_cast<volatile int*>(smem + 392);
   uint2* qtab = reinterpret_cast<uint2*>(smem + 512);  // KPS = 8: (hi, lo) half2 words of omega^m
   uint32_t* jt = reinterpret_cast<uint32_t*>(smem + HDR);
-  unsigned char* stage0 = smem + HDR + plan.gm_jt_bytes;
   const int MT = plan.gm_mt;
   const uint32_t A_BYTES = (uint32_t)MT * A_TILE;
-  const uint32_t STAGE = stage_bytes(MT, plan.gm_npmax);
+  const uint32_t B_SLOT = (uint32_t)plan.gm_npmax * KC * 2;
+  unsigned char* aring = smem + HDR + plan.gm_jt_bytes;
+  unsigned char* bring = aring + na * A_BYTES;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nprod = MT * TM;
@@ -227,22 +263,26 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
     tmem_relinquish();
   }
   if (tid == 0) {
-    for (int i = 0; i < MAX_STAGES; ++i) {
+    for (int i = 0; i < MAX_NB; ++i) {
       mbar_init(&bfull[i], 1);
+      mbar_init(&bempty[i], 1);
+    }
+    for (int i = 0; i < MAX_NA; ++i) {
       mbar_init(&afull[i], MT * 4);
-      mbar_init(&empty[i], 1);
+      mbar_init(&aempty[i], 1);
     }
     mbar_init(accf, 1);
-    *abort_flag = 0;
+    // the swizzled layout needs 1024-byte aligned atoms
+    *abort_flag = ((smem_u32(aring) | smem_u32(bring)) & 1023u) ? 1 : 0;
     *n_con = 0;
     fence_mbar_init();
   }
   if (KPS == 8 && tid < q) {
-    const double2 wr = root_of_unity(tid, q);
-    __half hr, lr, hi, li;
-    split_h(wr.x, hr, lr);
-    split_h(wr.y, hi, li);
-    qtab[tid] = make_uint2(h2_bits(hr, hi), h2_bits(lr, li));
+    const double* r = plan.roots + ((int64_t)q * 32 + tid) * 2;
+    const float wr = (float)r[0], wi = (float)r[1];
+    const __half hr = __float2half_rn(wr), hi = __float2half_rn(wi);
+    qtab[tid] = make_uint2(h2_bits(hr, hi), h2_bits(__float2half_rn(wr - __half2float(hr)),
+                                                    __float2half_rn(wi - __half2float(hi))));
   }
   for (int i = tid; i < g.S_pad * NW; i += blockDim.x) jt[i] = __ldg(gJ + i);
   tc_fence_before();
@@ -271,24 +311,25 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
       }
     }
     const ModQ mq = make_modq(q);
-    const uint32_t a_off = (uint32_t)t * A_TILE + (tr >> 3) * SBO + (tr & 7) * 16;
+    const uint32_t a_off = (uint32_t)t * A_TILE + (uint32_t)(tr >> 3) * 1024 + (uint32_t)(tr & 7) * 128;
+    const uint32_t sw = (uint32_t)(tr & 7) * 16;  // the row's chunk swizzle, as a byte XOR: sw128(tr, 8i)
     for (int kc = 0; kc < nK; ++kc) {
-      const int st = kc % ns;
-      const uint32_t ph = (uint32_t)(kc / ns) & 1;
+      const int st = kc % na;
+      const uint32_t ph = (uint32_t)(kc / na) & 1;
       int go = 1;
-      if (lane == 0) go = !*abort_flag && mbar_wait(&empty[st], ph ^ 1);
+      if (lane == 0) go = !*abort_flag && mbar_wait(&aempty[st], ph ^ 1);
       go = __shfl_sync(~0u, go, 0);
       if (!go) {
         if (lane == 0) *abort_flag = 1;
         break;
       }
-      unsigned char* ap = stage0 + st * STAGE + a_off;
+      unsigned char* ap = aring + st * A_BYTES + a_off;
       const int s0 = kc * (KC / KPS);
       if constexpr (KPS == 4) {
         // omega_4^m as half2 (re, im): high bytes from the tables 0x00BC003C (re)
         // and 0xBC003C00 (im), low bytes zero
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < 8; ++i) {
           const uint32_t* jp = jt + (s0 + 2 * i) * NW;
           uint32_t d0 = 0, d1 = 0;
 #pragma unroll
@@ -298,17 +339,17 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
           }
           const uint32_t w0 = __byte_perm(0x00BC003Cu, 0xBC003C00u, 0x4101u + (d0 & 3u) * 0x1010u);
           const uint32_t w1 = __byte_perm(0x00BC003Cu, 0xBC003C00u, 0x4101u + (d1 & 3u) * 0x1010u);
-          *reinterpret_cast<uint4*>(ap + i * 128) = make_uint4(w0, w0, w1, w1);
+          *reinterpret_cast<uint4*>(ap + ((i * 16) ^ sw)) = make_uint4(w0, w0, w1, w1);
         }
       } else {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < 8; ++i) {
           const uint32_t* jp = jt + (s0 + i) * NW;
           uint32_t d = 0;
 #pragma unroll
           for (int k = 0; k < NW; ++k) d = __dp4a(lw[k], jp[k], d);
           const uint2 h = qtab[modq(d, mq)];
-          *reinterpret_cast<uint4*>(ap + i * 128) = make_uint4(h.x, h.x, h.y, h.y);
+          *reinterpret_cast<uint4*>(ap + ((i * 16) ^ sw)) = make_uint4(h.x, h.x, h.y, h.y);
         }
       }
       fence_async_smem();
@@ -355,27 +396,31 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
       *abort_flag = 1;
     }
   } else if (warp == mma_warp) {
-    // ---- MMA issue
+    // ---- MMA issue.  Descriptors differ between stages, tiles and K steps
+    // only in the start-address field (smem address >> 4 < 2^14, no carry),
+    // so they are built once and offset.
     if (lane == 0) {
       const uint32_t idesc = tc::make_idesc(TM, g.NP);
+      const uint64_t a0 = desc_sw128(smem_u32(aring)), b0 = desc_sw128(smem_u32(bring));
       int con = 0;
       for (int kc = 0; kc < nK; ++kc) {
-        const int st = kc % ns;
-        const uint32_t ph = (uint32_t)(kc / ns) & 1;
+        const int sa = kc % na, sbi = kc % nb;
         if (*abort_flag) break;
-        if (!mbar_wait(&bfull[st], ph) || !mbar_wait(&afull[st], ph)) {
+        if (!mbar_wait(&bfull[sbi], (uint32_t)(kc / nb) & 1) || !mbar_wait(&afull[sa], (uint32_t)(kc / na) & 1)) {
           *abort_flag = 1;
           break;
         }
         tc_fence_after();
-        const uint32_t a_base = smem_u32(stage0 + st * STAGE), b_base = a_base + A_BYTES;
+        const uint64_t ad = a0 + ((sa * A_BYTES) >> 4), bd = b0 + ((sbi * B_SLOT) >> 4);
         for (int t = 0; t < MT; ++t) {
+          const uint32_t dt = tmem + (uint32_t)(t * g.NP);
+          const uint64_t at = ad + ((t * A_TILE) >> 4);
 #pragma unroll
-          for (int ks = 0; ks < KC / 16; ++ks)
-            mma_f16(tmem + (uint32_t)(t * g.NP), make_desc(a_base + t * A_TILE + ks * 256, 128, SBO),
-                    make_desc(b_base + ks * 256, 128, SBO), idesc, (kc | ks) > 0);
+          for (int ks = 0; ks < KC / 16; ++ks)  // K = 16 is 32 bytes along the swizzled row
+            mma_f16(dt, at + ks * 2, bd + ks * 2, idesc, (kc | ks) > 0);
         }
-        mma_commit(&empty[st]);
+        mma_commit(&aempty[sa]);
+        mma_commit(&bempty[sbi]);
         con = kc + 1;
       }
       mma_commit(accf);  // arrives once every MMA issued above has completed
@@ -383,18 +428,17 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
     }
     __syncwarp();
   } else if (warp == load_warp) {
-    // ---- B chunks: one bulk copy per stage
+    // ---- B chunks: one bulk copy per stage, up to nb in flight
     if (lane == 0) {
       for (int kc = 0; kc < nK; ++kc) {
-        const int st = kc % ns;
-        const uint32_t ph = (uint32_t)(kc / ns) & 1;
+        const int st = kc % nb;
         if (*abort_flag) break;
-        if (!mbar_wait(&empty[st], ph ^ 1)) {
+        if (!mbar_wait(&bempty[st], ((uint32_t)(kc / nb) & 1) ^ 1)) {
           *abort_flag = 1;
           break;
         }
         mbar_arrive_expect_tx(&bfull[st], g.CB);
-        bulk_g2s(stage0 + st * STAGE + A_BYTES, gB + (int64_t)kc * g.CB, g.CB, &bfull[st]);
+        bulk_g2s(bring + st * B_SLOT, gB + (int64_t)kc * g.CB, g.CB, &bfull[st]);
         iss = kc + 1;
       }
     }
@@ -403,7 +447,7 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
   __syncthreads();  // every role loop has ended; n_con is final
   if (warp == load_warp && lane == 0)
     for (int kc = *n_con; kc < iss; ++kc)  // copies that no MMA consumed: let them land (bounded)
-      mbar_wait(&bfull[kc % ns], (uint32_t)(kc / ns) & 1);
+      mbar_wait(&bfull[kc % nb], (uint32_t)(kc / nb) & 1);
   if (warp == mma_warp && lane == 0 && *abort_flag) mbar_wait(accf, 0);  // MMAs done before dealloc
   tc_fence_before();
   __syncthreads();
@@ -412,21 +456,29 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
   if (warp == mma_warp) tmem_dealloc(tmem, ncols);
 }
 
+// stage counts for the shared-memory budget: 4 A + 8 B stages, B first trimmed to 4
+inline bool pick_stages(int mt, int npmax, int jt_bytes, int& na, int& nb, int& smem) {
+  const int fixed = HDR + jt_bytes, ab = mt * (int)A_TILE, bb = npmax * KC * 2;
+  for (na = MAX_NA; na >= 2; --na)
+    for (nb = MAX_NB; nb >= 4; --nb)
+      if (fixed + na * ab + nb * bb <= MAX_SMEM) {
+        smem = fixed + na * ab + nb * bb;
+        return true;
+      }
+  return false;
+}
+
 template <int KPS, int NW>
 static int launch(const qsft_plan* p, cudaStream_t st) {
-  const uint32_t stage = stage_bytes(p->gm_mt, p->gm_npmax);
-  const int fixed = HDR + p->gm_jt_bytes;
-  int ns = (MAX_SMEM - fixed) / (int)stage;
-  if (ns > MAX_STAGES) ns = MAX_STAGES;
-  if (ns < 2) return QSFT_ERR_TOO_LARGE;
-  const int smem = fixed + ns * (int)stage;
+  int na, nb, smem;
+  if (!pick_stages(p->gm_mt, p->gm_npmax, p->gm_jt_bytes, na, nb, smem)) return QSFT_ERR_TOO_LARGE;
   if (p->total_gm_prep > 0) {
     gemm_prep_kernel<KPS, NW><<<(unsigned)p->total_gm_prep, 256, 0, st>>>(*p);
     QSFT_CUDA_CHECK_LAUNCH();
   }
   auto kern = eval_gemm_kernel<KPS, NW>;
   if (!ensure_smem((const void*)kern, smem)) return QSFT_ERR_CUDA;
-  kern<<<(unsigned)p->total_gm_work, p->gm_mt * TM + 64, smem, st>>>(*p, ns);
+  kern<<<(unsigned)p->total_gm_work, p->gm_mt * TM + 64, smem, st>>>(*p, na, nb);
   QSFT_CUDA_CHECK_LAUNCH();
   return QSFT_OK;
 }
@@ -462,7 +514,7 @@ extern "C" int qsft_gemm_layout(const qsft_job* jobs, int njobs, qsft_plan* plan
     npmax = npmax > np ? npmax : np;
   }
   const int nw = maxb <= 4 ? 1 : (maxb <= 8 ? 2 : 4);
-  int mt = gm::MAX_MT;
+  int mt = (plan->gm_mt == 1 || plan->gm_mt == 2) ? plan->gm_mt : gm::MAX_MT;
   while (mt > 1 && (mt * npmax > 512 || (int64_t)(mt / 2) * gm::TM >= maxB)) mt /= 2;
   int64_t work = 0, prep = 0, off = 0;
   index[0] = 0;
@@ -477,10 +529,11 @@ extern "C" int qsft_gemm_layout(const qsft_job* jobs, int njobs, qsft_plan* plan
     index[njobs + 2 + i] = prep;
     index[2 * (njobs + 1) + i] = off;
     off += gm::region_bytes(g, jb.C);
-    const int jtb = (g.S_pad * nw * 4 + 127) / 128 * 128;
+    const int jtb = (g.S_pad * nw * 4 + 1023) / 1024 * 1024;  // keeps the rings 1024-byte aligned
     jt = jt > jtb ? jt : jtb;
   }
-  if (gm::HDR + jt + 2 * (int)gm::stage_bytes(mt, npmax) > gm::MAX_SMEM) return QSFT_ERR_TOO_LARGE;
+  int na, nb, smem;
+  if (!gm::pick_stages(mt, npmax, jt, na, nb, smem)) return QSFT_ERR_TOO_LARGE;
   if (work > 0x7fffffffLL || prep > 0x7fffffffLL) return QSFT_ERR_TOO_LARGE;
   plan->gm_mt = mt;
   plan->gm_kps = kps;
