@@ -126,14 +126,16 @@ typedef struct qsft_plan {
   const int32_t* gf_tables;    /* RS: exp | log | zech tables per field             */
   const double* roots;         /* exp(2 pi i m / q) at ((q*32 + m)*2), q <= 32      */
   /* peeling workspace (sizes from qsft_workspace_layout) */
-  uint8_t* kbuf;               /* [total_bins * kstride]   decoded k per bin        */
-  double* rho;                 /* [total_bins * 2]         FP64 coefficient per bin */
-  /* per-iteration dedupe table; entries are stamped with the iteration number
-   * in their high 32 bits so that no clearing is needed between iterations   */
-  int64_t* tab_key;            /* [total_slots]  (iter << 32) | (local bin + 1)     */
-  int64_t* tab_best;           /* [total_slots]  (iter << 32) | max local bin       */
-  int32_t* uniq;               /* [total_slots]  per-job list of occupied slots     */
-  int32_t* ball_tab;           /* [total_slots]  persistent k -> ball id + 1        */
+  uint8_t* kbuf;               /* [total_bins * kstride] decoded k per singleton bin */
+  double* rho;                 /* [total_bins * 2]   FP64 coefficient per singleton bin */
+  /* persistent hash table k -> ball: (tag << 32) | (ball id + 1), tag a
+   * nonzero 32-bit hash of k, so that probes compare k rows only on a tag hit */
+  int64_t* ball_tab;           /* [total_slots]                                     */
+  /* (iteration << 32) | largest local bin among the iteration's detections of
+   * the ball: no clearing between iterations, and the atomicMax that records
+   * a detection also tells whether it is the ball's first in the iteration   */
+  int64_t* ball_best;          /* [total_balls]                                     */
+  int32_t* uniq;               /* [total_balls]  balls detected in this iteration   */
   uint8_t* ball_k;             /* [total_balls * kstride]                           */
   double* ball_sum;            /* [total_balls * 2]                                 */
   int32_t* ball_cnt;           /* [total_balls]                                     */
@@ -282,7 +284,15 @@ int qsft_peel_init(const qsft_plan* plan, qsft_stream_t stream);
  * function of the bin's unchanged values, so the outcome is the same.
  */
 int qsft_peel_iteration(const qsft_plan* plan, int first, qsft_stream_t stream);
-/* max_iter iterations back to back (iterations of finished jobs are no-ops) */
+/* kernels one peeling iteration launches (scan, decode, record, peel, iter_end) */
+#define QSFT_PEEL_LAUNCHES_PER_ITER 5
+/*
+ * Up to max_iter iterations.  Issued eagerly, all max_iter are launched
+ * (iterations of finished jobs are no-ops).  Inside a stream capture,
+ * iteration 1 is captured and iterations 2.. become one conditional WHILE
+ * node of the graph whose body runs only while some job is still in its loop
+ * (the condition is set on the device at the end of every iteration).
+ */
 int qsft_peel_run(const qsft_plan* plan, int max_iter, qsft_stream_t stream);
 
 /*
@@ -321,7 +331,7 @@ int qsft_rs_decode(int q, int s, int t, int n, const int32_t* gf_tables, const u
  * cudaMalloc's device-wide synchronisation, plugin hosts that own every
  * buffer.  All scratch (hash tables, result store, lists, roots table, control
  * record) lives in a statically sized device array inside the library (about
- * 2.9 MB, held by every GPU that loads the library until the process exits),
+ * 2.4 MB, held by every GPU that loads the library until the process exits),
  * so the call allocates nothing.  `job` is a host record (offsets off_M/off_D
  * into i8, off_U into U; qsft_workspace_layout's fields are filled in by the
  * call); U holds the job's bins and is peeled in place.  Results as

@@ -36,11 +36,10 @@ constexpr size_t OFF_CTRL = al(OFF_INDEX + 2 * sizeof(int64_t));
 constexpr size_t OFF_DONE = al(OFF_CTRL + sizeof(qsft_ctrl));
 constexpr size_t OFF_KBUF = al(OFF_DONE + sizeof(int32_t));
 constexpr size_t OFF_RHO = al(OFF_KBUF + MAX_BINS * KSTRIDE);
-constexpr size_t OFF_TABKEY = al(OFF_RHO + MAX_BINS * 2 * sizeof(double));
-constexpr size_t OFF_TABBEST = al(OFF_TABKEY + MAX_SLOTS * sizeof(int64_t));
-constexpr size_t OFF_UNIQ = al(OFF_TABBEST + MAX_SLOTS * sizeof(int64_t));
-constexpr size_t OFF_BALLTAB = al(OFF_UNIQ + MAX_SLOTS * sizeof(int32_t));
-constexpr size_t OFF_BALLK = al(OFF_BALLTAB + MAX_SLOTS * sizeof(int32_t));
+constexpr size_t OFF_BALLTAB = al(OFF_RHO + MAX_BINS * 2 * sizeof(double));
+constexpr size_t OFF_BALLBEST = al(OFF_BALLTAB + MAX_SLOTS * sizeof(int64_t));
+constexpr size_t OFF_UNIQ = al(OFF_BALLBEST + MAX_BALLS * sizeof(int64_t));
+constexpr size_t OFF_BALLK = al(OFF_UNIQ + MAX_BALLS * sizeof(int32_t));
 constexpr size_t OFF_BALLSUM = al(OFF_BALLK + MAX_BALLS * KSTRIDE);
 constexpr size_t OFF_BALLCNT = al(OFF_BALLSUM + MAX_BALLS * 2 * sizeof(double));
 constexpr size_t OFF_STATUS = al(OFF_BALLCNT + MAX_BALLS * sizeof(int32_t));
@@ -133,10 +132,9 @@ extern "C" int qsft_peel_noalloc(int prec, const qsft_job* job_in, const int8_t*
   p.roots = reinterpret_cast<const double*>(base + OFF_ROOTS);
   p.kbuf = base + OFF_KBUF;
   p.rho = reinterpret_cast<double*>(base + OFF_RHO);
-  p.tab_key = reinterpret_cast<int64_t*>(base + OFF_TABKEY);
-  p.tab_best = reinterpret_cast<int64_t*>(base + OFF_TABBEST);
+  p.ball_tab = reinterpret_cast<int64_t*>(base + OFF_BALLTAB);
+  p.ball_best = reinterpret_cast<int64_t*>(base + OFF_BALLBEST);
   p.uniq = reinterpret_cast<int32_t*>(base + OFF_UNIQ);
-  p.ball_tab = reinterpret_cast<int32_t*>(base + OFF_BALLTAB);
   p.ball_k = base + OFF_BALLK;
   p.ball_sum = reinterpret_cast<double*>(base + OFF_BALLSUM);
   p.ball_cnt = reinterpret_cast<int32_t*>(base + OFF_BALLCNT);

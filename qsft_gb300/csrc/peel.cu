@@ -1,7 +1,7 @@
 // Singleton detection and peeling: QSFT.transform's while-loop
 // (qsft/qsft.py:151-255) for a batch of transforms.
 //
-// One iteration = four launches:
+// One iteration = five launches:
 //   scan          thread per bin: the zeroton test ||col||^2 > cutoff*len
 //                 (qsft/qsft.py:164); bins above it are queued.  The first
 //                 iteration scans every bin; later ones only the bins that the
@@ -11,22 +11,25 @@
 //   decode        warp per queued bin: channel decoding of k (noiseless
 //                 qsft/reconstruct.py:12-31 or NSO "nso1" :100-113, lanes over
 //                 symbols), optional Reed-Solomon source decoding (:34-51),
-//                 FP64 projection rho = <omega^(Dk), col>/len and FP64 residual
+//                 projection rho = <omega^(Dk), col>/len and residual energy
 //                 (lanes over rows, warp reductions), bin-match test
-//                 (qsft/qsft.py:174-190).  Singletons are deduplicated by k in a
-//                 per-iteration hash table that keeps the largest (group, bin)
-//                 -- the reference's dict order, `ball_values` (:209-216) -- and
-//                 their rho goes to the job's result store (the `result` list
-//                 and its running mean, :217, 247-255).
-//   peel          warp per distinct k: subtract rho * omega^(D_l k) from bin
-//                 M_l^T k (mod q) of every group l (qsft/qsft.py:223-241) and
-//                 queue each changed bin for the next scan.
+//                 (qsft/qsft.py:174-190); singletons leave k and rho behind.
+//   record        thread per queued bin: each singleton finds (or creates)
+//                 the ball of its k in a persistent hash table, adds its rho to
+//                 the ball's running sum (the `result` list and its mean,
+//                 :217, 247-255) and marks the ball detected in this iteration
+//                 keeping the largest (group, bin) -- the reference's dict
+//                 order, `ball_values` (:209-216).
+//   peel          thread per (detected ball, group l): subtract
+//                 rho * omega^(D_l k) from bin M_l^T k (mod q) of group l
+//                 (qsft/qsft.py:223-241) and queue the changed bin for the
+//                 next scan.
 //   iter_end      per job: iteration count, cumulative peel count and the
 //                 loop's stopping rules (qsft/qsft.py:151, 204-205).
 //
-// FP32 data path: bins are stored as float2.  Energy and phase decisions that
-// fall within a small band of their thresholds are recomputed in FP64; the
-// coefficient projection and residual energy are always computed in FP64.
+// FP32 data path: bins are stored as float2.  Energy, phase and residual
+// decisions that fall within a small band of their thresholds are recomputed
+// in FP64 (GB300's FP64 rate is a small fraction of its FP32 rate).
 #include "common.cuh"
 #include "rs.cuh"
 
@@ -50,14 +53,6 @@ __device__ __forceinline__ uint32_t hash_row(const uint8_t* row, int words) {
   h ^= h >> 32;
   return (uint32_t)h;
 }
-// compare our row with a row another warp wrote (read through L2)
-__device__ __forceinline__ bool row_eq(const uint8_t* mine, const uint8_t* other, int words) {
-  const uint32_t* a = reinterpret_cast<const uint32_t*>(mine);
-  const uint32_t* b = reinterpret_cast<const uint32_t*>(other);
-  for (int i = 0; i < words; ++i)
-    if (a[i] != __ldcg(b + i)) return false;
-  return true;
-}
 __device__ __forceinline__ double2 root(const double* roots, int q, int m) {
   return make_double2(__ldg(roots + (q * 32 + m) * 2), __ldg(roots + (q * 32 + m) * 2 + 1));
 }
@@ -74,6 +69,11 @@ __device__ __forceinline__ int nearest_root(double ang, int q) {
     }
   }
   return best % q;
+}
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
 }
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -174,16 +174,46 @@ __global__ void __launch_bounds__(SCAN_THREADS) scan_dirty_kernel(qsft_plan plan
 }
 
 // ---------------------------------------------------------------- decode
+constexpr int STAGE_RP = 128;  // columns of up to this many rows are staged in shared memory
+
+// phase <d, k> mod q of delay row d (n digits) against k (kstride-padded bytes)
+__device__ __forceinline__ int row_phase(const int8_t* dr, const uint8_t* kl, int n, bool words_ok, int q) {
+  int ph = 0;
+  if (words_ok) {
+    const uint32_t* dw = reinterpret_cast<const uint32_t*>(dr);
+    const uint32_t* kw = reinterpret_cast<const uint32_t*>(kl);
+    for (int w = 0; w < (n >> 2); ++w) ph = (int)__dp4a((unsigned)__ldg(dw + w), (unsigned)kw[w], (unsigned)ph);
+  } else {
+    for (int i = 0; i < n; ++i) ph += (int)dr[i] * (int)kl[i];
+  }
+  return ph % q;
+}
+
+// k rows (kstride bytes, 16-byte multiples) compared with 16-byte loads through L2
+__device__ __forceinline__ bool krow_eq(const uint8_t* mine, const uint8_t* other, int ks) {
+  const uint4* a = reinterpret_cast<const uint4*>(mine);
+  const uint4* b = reinterpret_cast<const uint4*>(other);
+  bool eq = true;
+  for (int i = 0; i < ks / 16; ++i) {
+    const uint4 x = a[i], y = __ldcg(b + i);
+    eq &= (x.x == y.x) & (x.y == y.y) & (x.z == y.z) & (x.w == y.w);
+  }
+  return eq;
+}
+
 template <typename T>
-__global__ void __launch_bounds__(WARPS_PER_BLOCK * 32) decode_kernel(qsft_plan plan) {
+__global__ void __launch_bounds__(WARPS_PER_BLOCK * 32, 3) decode_kernel(qsft_plan plan) {
   if (__ldcg(plan.done_count) >= plan.njobs) return;  // every job has left the loop
   __shared__ __align__(16) uint8_t s_k[WARPS_PER_BLOCK][QSFT_MAX_N + 16];
   __shared__ uint8_t s_sym[WARPS_PER_BLOCK][MAX_SYMS];
+  __shared__ c2<T> s_col[WARPS_PER_BLOCK][STAGE_RP];
+  __shared__ float2 s_w[WARPS_PER_BLOCK][QSFT_MAX_Q];  // exp(2 pi i m / q) of the current job, FP32
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int gw = blockIdx.x * WARPS_PER_BLOCK + wib;
   const int nw = gridDim.x * WARPS_PER_BLOCK;
   uint8_t* kl = s_k[wib];
   uint8_t* syms = s_sym[wib];
+  c2<T>* sc = s_col[wib];
   int64_t base = 0;  // items of all jobs are dealt round-robin to the warps of the grid
   for (int jid = 0; jid < plan.njobs; ++jid) {
     qsft_ctrl* ctl = plan.ctrl + jid;
@@ -196,19 +226,28 @@ __global__ void __launch_bounds__(WARPS_PER_BLOCK * 32) decode_kernel(qsft_plan 
     const int q = job->q, n = job->n, b = job->b, B = job->B, P = job->P, R = job->R;
     const int RP = R * P, nsym = P - 1;
     const double thr = job->cutoff * RP;
-    const int ks = plan.kstride, words = ks / 4;
-    const long long iter = (long long)ctl->iter + 1;
+    const int ks = plan.kstride;
+    const bool staged = RP <= STAGE_RP;
+    const bool words_ok = (n & 3) == 0 && ((job->off_D & 3) == 0);
+    if (lane < q) s_w[wib][lane] = make_float2((float)plan.roots[(q * 32 + lane) * 2], (float)plan.roots[(q * 32 + lane) * 2 + 1]);
+    __syncwarp();
     for (int u = start; u < cnt; u += nw) {
       const int local = plan.cand[job->off_bin + u];
       const int c = local / B, jb = local - (local / B) * B;
       const int64_t gb = job->off_bin + local;
       const c2<T>* col = reinterpret_cast<const c2<T>*>(plan.U) + job->off_U + (int64_t)c * RP * B + jb;
+      // the column's RP values (stride B) in one round of loads
+      if (staged) {
+        for (int r = lane; r < RP; r += 32) sc[r] = col[(int64_t)r * B];
+        __syncwarp();
+      }
+      auto V = [&](int r) -> c2<T> { return staged ? sc[r] : col[(int64_t)r * B]; };
       // ---- channel decoding, lanes over symbols
       if (job->chan == QSFT_CHAN_IDENTITY) {
-        const c2<T> v0 = col[0];
+        const c2<T> v0 = V(0);
         const T a0 = atan2(v0.y, v0.x);
         for (int i = lane + 1; i < RP && i <= nsym; i += 32) {
-          const c2<T> vi = col[(int64_t)i * B];
+          const c2<T> vi = V(i);
           const T ai = atan2(vi.y, vi.x);
           double a = (double)((T)q * (ai - a0) / (T)6.283185307179586);
           if (sizeof(T) == 4 && fabs(a - floor(a) - 0.5) < 1e-3)
@@ -223,8 +262,7 @@ __global__ void __launch_bounds__(WARPS_PER_BLOCK * 32) decode_kernel(qsft_plan 
         for (int i = lane + 1; i <= nsym; i += 32) {
           T zr = 0, zi = 0;
           for (int r = 0; r < R; ++r) {
-            const c2<T> u0 = col[(int64_t)(r * P) * B];
-            const c2<T> ui = col[(int64_t)(r * P + i) * B];
+            const c2<T> u0 = V(r * P), ui = V(r * P + i);
             zr += u0.x * ui.x + u0.y * ui.y;
             zi += u0.y * ui.x - u0.x * ui.y;
           }
@@ -239,8 +277,7 @@ __global__ void __launch_bounds__(WARPS_PER_BLOCK * 32) decode_kernel(qsft_plan 
             }
             double dzr = 0, dzi = 0;  // near a rounding boundary: recompute in FP64
             for (int r = 0; r < R; ++r) {
-              const double2 u0 = to_d2(col[(int64_t)(r * P) * B]);
-              const double2 ui = to_d2(col[(int64_t)(r * P + i) * B]);
+              const double2 u0 = to_d2(V(r * P)), ui = to_d2(V(r * P + i));
               dzr += u0.x * ui.x + u0.y * ui.y;
               dzi += u0.y * ui.x - u0.x * ui.y;
             }
@@ -267,60 +304,73 @@ __global__ void __launch_bounds__(WARPS_PER_BLOCK * 32) decode_kernel(qsft_plan 
       __syncwarp();
       for (int i = n + lane; i < ks; i += 32) kl[i] = 0;
       __syncwarp();
-      // ---- FP64 projection and residual, lanes over rows (phases <d_r, k> mod q
-      //      of the first 4*32 rows kept in registers between the two passes)
+      // ---- projection rho = <omega^(Dk), col> / RP and residual energy, lanes
+      //      over rows (phases of the first 4*32 rows kept in registers).
+      //      FP64 plans compute both in FP64; FP32 plans in FP32 (their bins
+      //      are FP32), recomputing in FP64 when the residual falls within 1%
+      //      of the singleton threshold.
       const int8_t* Dc = plan.i8 + job->off_D + (int64_t)c * RP * n;
-      const bool words_ok = (n & 3) == 0 && ((job->off_D & 3) == 0);
-      auto phase = [&](int r) -> int {
-        const int8_t* dr = Dc + (int64_t)r * n;
-        int ph = 0;
-        if (words_ok) {
-          const uint32_t* dw = reinterpret_cast<const uint32_t*>(dr);
-          const uint32_t* kw = reinterpret_cast<const uint32_t*>(kl);
-          for (int w = 0; w < (n >> 2); ++w) ph = (int)__dp4a((unsigned)__ldg(dw + w), (unsigned)kw[w], (unsigned)ph);
-        } else {
-          for (int i = 0; i < n; ++i) ph += (int)dr[i] * (int)kl[i];
-        }
-        return ph % q;
-      };
       int phc[4];
-      double ar = 0, ai = 0;
 #pragma unroll
       for (int k = 0; k < 4; ++k) {
         const int r = lane + 32 * k;
-        phc[k] = 0;
-        if (r < RP) {
-          phc[k] = phase(r);
-          const double2 w = root(plan.roots, q, phc[k]);
-          const double2 v = to_d2(col[(int64_t)r * B]);
+        phc[k] = r < RP ? row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q) : 0;
+      }
+      auto each_row = [&](auto&& f) {  // f(phase, row) over this lane's rows
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+          if (lane + 32 * k < RP) f(phc[k], lane + 32 * k);
+        for (int r = lane + 128; r < RP; r += 32) f(row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q), r);
+      };
+      auto project64 = [&](double2& rho_out, double& res_out) {
+        double ar = 0, ai = 0;
+        each_row([&](int ph, int r) {
+          const double2 w = root(plan.roots, q, ph);
+          const double2 v = to_d2(V(r));
           ar += w.x * v.x + w.y * v.y;
           ai += w.x * v.y - w.y * v.x;
-        }
-      }
-      for (int r = lane + 128; r < RP; r += 32) {
-        const double2 w = root(plan.roots, q, phase(r));
-        const double2 v = to_d2(col[(int64_t)r * B]);
-        ar += w.x * v.x + w.y * v.y;
-        ai += w.x * v.y - w.y * v.x;
-      }
-      ar = warp_sum(ar);
-      ai = warp_sum(ai);
-      const double2 rho = make_double2(ar / RP, ai / RP);
-      double res = 0;
-      auto resid = [&](int r, int ph) {
-        const double2 w = root(plan.roots, q, ph);
-        const double2 v = to_d2(col[(int64_t)r * B]);
-        const double dx = v.x - (rho.x * w.x - rho.y * w.y);
-        const double dy = v.y - (rho.x * w.y + rho.y * w.x);
-        res += dx * dx + dy * dy;
+        });
+        ar = warp_sum(ar);
+        ai = warp_sum(ai);
+        const double2 rh = make_double2(ar / RP, ai / RP);
+        double rs = 0;
+        each_row([&](int ph, int r) {
+          const double2 w = root(plan.roots, q, ph);
+          const double2 v = to_d2(V(r));
+          const double dx = v.x - (rh.x * w.x - rh.y * w.y);
+          const double dy = v.y - (rh.x * w.y + rh.y * w.x);
+          rs += dx * dx + dy * dy;
+        });
+        rho_out = rh;
+        res_out = warp_sum(rs);
       };
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const int r = lane + 32 * k;
-        if (r < RP) resid(r, phc[k]);
+      double2 rho;
+      double res;
+      if (sizeof(T) == 4) {
+        const float2* wt = s_w[wib];
+        float ar = 0.f, ai = 0.f;
+        each_row([&](int ph, int r) {
+          const float2 w = wt[ph];
+          const c2<T> v = V(r);
+          ar += w.x * (float)v.x + w.y * (float)v.y;
+          ai += w.x * (float)v.y - w.y * (float)v.x;
+        });
+        ar = warp_sum_f(ar) / (float)RP;
+        ai = warp_sum_f(ai) / (float)RP;
+        float rs = 0.f;
+        each_row([&](int ph, int r) {
+          const float2 w = wt[ph];
+          const c2<T> v = V(r);
+          const float dx = (float)v.x - (ar * w.x - ai * w.y);
+          const float dy = (float)v.y - (ar * w.y + ai * w.x);
+          rs += dx * dx + dy * dy;
+        });
+        rho = make_double2(ar, ai);
+        res = warp_sum_f(rs);
+        if (fabs(res - thr) <= 1e-2 * thr) project64(rho, res);  // warp-uniform: res is a warp sum
+      } else {
+        project64(rho, res);
       }
-      for (int r = lane + 128; r < RP; r += 32) resid(r, phase(r));
-      res = warp_sum(res);
       // ---- bin match: M_c^T k = digits of j (MSB first), lanes over the b digits
       bool ok = true;
       if (lane < b) {
@@ -333,193 +383,229 @@ __global__ void __launch_bounds__(WARPS_PER_BLOCK * 32) decode_kernel(qsft_plan 
       }
       const bool match = __all_sync(0xffffffffu, ok);
       const bool single = match && !(res > thr);
-      if (lane == 0) plan.bin_status[gb] = single ? 2 : 1;
-      if (!single) {
-        if (lane == 0) atomicAdd(&ctl->n_multi, 1);
-        __syncwarp();
-        continue;
-      }
-      // ---- singleton: record k and rho, dedupe, add to the result store
-      uint8_t* krow = plan.kbuf + gb * ks;
-      for (int w = lane; w < words; w += 32)
-        reinterpret_cast<uint32_t*>(krow)[w] = reinterpret_cast<const uint32_t*>(kl)[w];
-      if (lane == 0) {
-        plan.rho[2 * gb] = rho.x;
-        plan.rho[2 * gb + 1] = rho.y;
-      }
-      __threadfence();
-      __syncwarp();
-      if (lane == 0) {
-        atomicAdd(&ctl->n_single, 1);
-        const uint32_t h = hash_row(kl, words);
-        const int64_t cap = job->table_cap, mask = cap - 1;
-        const long long stamp = iter << 32;
-        unsigned long long* tk = reinterpret_cast<unsigned long long*>(plan.tab_key + job->off_slot);
-        int64_t slot = h & mask;
-        bool found = false, owner = false;
-        for (int64_t probe = 0; probe < cap && !found; ++probe) {
-          unsigned long long cur = atomicAdd(tk + slot, 0ull);
-          if ((long long)(cur >> 32) != iter) {
-            const unsigned long long mine = (unsigned long long)(stamp | (local + 1));
-            const unsigned long long prev = atomicCAS(tk + slot, cur, mine);
-            if (prev == cur) {
-              owner = found = true;
-              break;
-            }
-            cur = prev;
-          }
-          if ((long long)(cur >> 32) == iter) {
-            const int64_t ob = (int64_t)(cur & 0xffffffffull) - 1;
-            if (row_eq(kl, plan.kbuf + (job->off_bin + ob) * ks, words)) {
-              found = true;
-              break;
-            }
-            slot = (slot + 1) & mask;
-          }
+      if (single) {  // k, rho and the class for the record kernel
+        for (int w = lane; w < ks / 16; w += 32)
+          reinterpret_cast<uint4*>(plan.kbuf + gb * ks)[w] = reinterpret_cast<const uint4*>(kl)[w];
+        if (lane == 0) {
+          plan.rho[2 * gb] = rho.x;
+          plan.rho[2 * gb + 1] = rho.y;
         }
-        if (!found) {
-          atomicExch(&ctl->err, (int)QSFT_ERR_OVERFLOW);
-        } else {
-          if (owner) {
-            const int uix = atomicAdd(&ctl->n_unique, 1);
-            plan.uniq[job->off_slot + uix] = (int32_t)slot;
-          }
-          atomicMax(reinterpret_cast<unsigned long long*>(plan.tab_best + job->off_slot + slot),
-                    (unsigned long long)(stamp | local));
-          int32_t* bt = plan.ball_tab + job->off_slot;
-          int64_t s2 = h & mask;
-          int myid = -1, bid = -1;
-          for (int64_t probe = 0; probe < cap; ++probe) {
-            int cur = atomicAdd(bt + s2, 0);
+      }
+      if (lane == 0) {
+        plan.bin_status[gb] = single ? 2 : 1;
+        atomicAdd(single ? &ctl->n_single : &ctl->n_multi, 1);
+      }
+      __syncwarp();
+    }
+  }
+}
+
+// ---------------------------------------------------------------- record
+// Thread per queued bin; singletons (bin_status 2, k in kbuf, rho in rho) are
+// recorded: each finds (or creates) the ball of its k in the persistent table
+// (tags first, k rows only on a tag hit), adds rho to the ball's running sum,
+// and marks the ball detected in this iteration with (iteration << 32 | local)
+// by atomicMax -- the largest local bin wins, the reference's last-write order
+// over (group, bin) (qsft/qsft.py:209-216) -- appending the ball to the
+// iteration's list on its first detection.  A warp works on 32 bins of one
+// job at once, so the table's L2 round trips overlap.
+__global__ void __launch_bounds__(SCAN_THREADS) record_kernel(qsft_plan plan) {
+  if (__ldcg(plan.done_count) >= plan.njobs) return;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gw = tid >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  const int ks = plan.kstride;
+  int64_t chunk0 = 0;  // 32-entry chunks of all jobs' lists are dealt round-robin to the warps
+  for (int jid = 0; jid < plan.njobs; ++jid) {
+    qsft_ctrl* ctl = plan.ctrl + jid;
+    if (ctl->done) continue;
+    const int cnt = ctl->n_cand;
+    const int nch = (cnt + 31) >> 5;
+    const int start = (int)(((int64_t)gw - chunk0) % nw + nw) % nw;
+    chunk0 += nch;
+    if (start >= nch) continue;
+    const qsft_job* __restrict__ job = plan.jobs + jid;
+    const long long iter = (long long)ctl->iter + 1;
+    const int64_t mask = job->table_cap - 1;
+    unsigned long long* tab = reinterpret_cast<unsigned long long*>(plan.ball_tab + job->off_slot);
+    for (int ch = start; ch < nch; ch += nw) {
+      const int i = ch * 32 + (tid & 31);
+      bool first = false;
+      int bid = -1;
+      if (i < cnt) {
+        const int local = plan.cand[job->off_bin + i];
+        const int64_t gb = job->off_bin + local;
+        if (plan.bin_status[gb] == 2) {
+          const uint8_t* kr = plan.kbuf + gb * ks;
+          const uint32_t h = hash_row(kr, ks / 4);
+          const unsigned long long tag = (unsigned long long)(h | 1u) << 32;
+          int64_t slot = h & mask;
+          int myid = -1;
+          for (int64_t probe = 0; probe < job->table_cap; ++probe) {
+            unsigned long long cur = __ldcg(tab + slot);
             if (cur == 0) {
-              if (myid < 0) {
+              if (myid < 0) {  // publish our k row before the slot that points at it
                 myid = atomicAdd(&ctl->n_balls, 1);
                 if (myid >= job->ball_cap) break;
-                uint32_t* dst = reinterpret_cast<uint32_t*>(plan.ball_k + (job->off_ball + myid) * ks);
-                for (int w = 0; w < words; ++w) dst[w] = reinterpret_cast<const uint32_t*>(kl)[w];
+                const uint4* src = reinterpret_cast<const uint4*>(kr);
+                uint4* dst = reinterpret_cast<uint4*>(plan.ball_k + (job->off_ball + myid) * ks);
+                for (int w = 0; w < ks / 16; ++w) dst[w] = src[w];
                 __threadfence();
               }
-              const int prev = atomicCAS(bt + s2, 0, myid + 1);
+              const unsigned long long prev = atomicCAS(tab + slot, 0ull, tag | (unsigned long long)(myid + 1));
               if (prev == 0) {
                 bid = myid;
                 break;
               }
               cur = prev;
             }
-            if (row_eq(kl, plan.ball_k + (job->off_ball + cur - 1) * ks, words)) {
-              bid = cur - 1;
-              break;
+            if ((cur & 0xffffffff00000000ull) == tag) {
+              const int other = (int)(cur & 0xffffffffull) - 1;
+              if (krow_eq(kr, plan.ball_k + (job->off_ball + other) * ks, ks)) {
+                bid = other;
+                break;
+              }
             }
-            s2 = (s2 + 1) & mask;
+            slot = (slot + 1) & mask;
           }
           if (bid < 0) {
             atomicExch(&ctl->err, (int)QSFT_ERR_OVERFLOW);
           } else {
-            atomicAdd(plan.ball_sum + 2 * (job->off_ball + bid), rho.x);
-            atomicAdd(plan.ball_sum + 2 * (job->off_ball + bid) + 1, rho.y);
-            atomicAdd(plan.ball_cnt + job->off_ball + bid, 1);
+            // a ball id allocated for a k that another thread inserted first
+            // stays an empty row (count 0): the collection skips it
+            const int64_t gball = job->off_ball + bid;
+            atomicAdd(plan.ball_sum + 2 * gball, plan.rho[2 * gb]);
+            atomicAdd(plan.ball_sum + 2 * gball + 1, plan.rho[2 * gb + 1]);
+            atomicAdd(plan.ball_cnt + gball, 1);
+            const unsigned long long old = atomicMax(reinterpret_cast<unsigned long long*>(plan.ball_best) + gball,
+                                                     (unsigned long long)((iter << 32) | (unsigned)local));
+            first = (long long)(old >> 32) != iter;
           }
         }
       }
-      __syncwarp();
+      const int pos = warp_append(first, jid, &ctl->n_unique);
+      if (first) plan.uniq[job->off_ball + pos] = bid;
     }
   }
 }
 
 // ---------------------------------------------------------------- peel
+// one bin-entry subtraction: U -= (dx, dy)
+__device__ __forceinline__ void sub_entry(float2* p, float dx, float dy) {
+  asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(-dx), "f"(-dy) : "memory");
+}
+__device__ __forceinline__ void sub_entry(double2* p, double dx, double dy) {
+  atomicAdd(&p->x, -dx);
+  atomicAdd(&p->y, -dy);
+}
+
+// Thread per (ball detected in the iteration, group l): subtract
+// rho * omega^(<d_r, k>) from every row r of bin M_l^T k (mod q) of group l
+// and queue the bin for the next scan.  FP32 plans rotate rho in FP32: the
+// entries it is subtracted from are FP32.
 template <typename T>
-__global__ void __launch_bounds__(WARPS_PER_BLOCK * 32) peel_kernel(qsft_plan plan) {
+__global__ void __launch_bounds__(SCAN_THREADS) peel_kernel(qsft_plan plan) {
   if (__ldcg(plan.done_count) >= plan.njobs) return;  // every job has left the loop
-  __shared__ uint8_t sk[WARPS_PER_BLOCK][QSFT_MAX_N];
-  const int lane = threadIdx.x & 31;
-  const int wib = threadIdx.x >> 5;
-  const int gw = blockIdx.x * WARPS_PER_BLOCK + wib;
-  const int nw = gridDim.x * WARPS_PER_BLOCK;
-  int64_t base = 0;  // balls of all jobs are dealt round-robin to the warps of the grid
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int gw = tid >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  const int ks = plan.kstride;
+  int64_t chunk0 = 0;
   for (int jid = 0; jid < plan.njobs; ++jid) {
     qsft_ctrl* ctl = plan.ctrl + jid;
     if (ctl->done) continue;
-    const int cnt = ctl->n_unique;
-    const int start = (int)(((int64_t)gw - base) % nw + nw) % nw;
-    base += cnt;
-    if (start >= cnt) continue;
     const qsft_job* __restrict__ job = plan.jobs + jid;
-    const int q = job->q, n = job->n, b = job->b, B = job->B, C = job->C;
+    const int C = job->C;
+    const int cnt = ctl->n_unique * C;
+    const int nch = (cnt + 31) >> 5;
+    const int start = (int)(((int64_t)gw - chunk0) % nw + nw) % nw;
+    chunk0 += nch;
+    if (start >= nch) continue;
+    const int q = job->q, n = job->n, b = job->b, B = job->B;
     const int RP = job->R * job->P;
     const int iter = ctl->iter + 1;
     const int parity = iter & 1;
+    const bool words_ok = (n & 3) == 0 && ((job->off_D & 3) == 0);
     int32_t* list = plan.dirty + (int64_t)parity * plan.total_bins + job->off_bin;
-    for (int u = start; u < cnt; u += nw) {
-      const int slot = plan.uniq[job->off_slot + u];
-      const unsigned long long key = __ldcg(reinterpret_cast<const unsigned long long*>(plan.tab_key + job->off_slot) + slot);
-      const unsigned long long best = __ldcg(reinterpret_cast<const unsigned long long*>(plan.tab_best + job->off_slot) + slot);
-      const int64_t owner = (int64_t)(key & 0xffffffffull) - 1;
-      const int64_t bestb = (int64_t)(best & 0xffffffffull);
-      const uint8_t* krow = plan.kbuf + (job->off_bin + owner) * plan.kstride;
-      for (int i = lane; i < n; i += 32) sk[wib][i] = __ldcg(krow + i);
-      __syncwarp();
-      const double2 rho = make_double2(__ldcg(plan.rho + 2 * (job->off_bin + bestb)),
-                                       __ldcg(plan.rho + 2 * (job->off_bin + bestb) + 1));
-      for (int l = 0; l < C; ++l) {
+    for (int ch = start; ch < nch; ch += nw) {
+      const int it = ch * 32 + (tid & 31);
+      bool fresh = false;
+      int lb = 0;
+      if (it < cnt) {
+        const int u = it / C, l = it - (it / C) * C;
+        const int bid = __ldcg(plan.uniq + job->off_ball + u);
+        const int64_t gball = job->off_ball + bid;
+        const unsigned long long best = __ldcg(reinterpret_cast<const unsigned long long*>(plan.ball_best) + gball);
+        const int64_t gbest = job->off_bin + (int64_t)(best & 0xffffffffull);
+        const double2 rho = make_double2(__ldcg(plan.rho + 2 * gbest), __ldcg(plan.rho + 2 * gbest + 1));
+        const uint8_t* kl = plan.ball_k + gball * ks;  // written by the record kernel
         const int8_t* Ml = plan.i8 + job->off_M + (int64_t)l * n * b;
-        int contrib = 0;
-        if (lane < b) {
+        int jl = 0;
+        for (int t = 0; t < b; ++t) {  // bin index, MSB-first digits of M_l^T k
           int dg = 0;
-          for (int i = 0; i < n; ++i) dg += (int)Ml[i * b + lane] * (int)sk[wib][i];
-          dg %= q;
-          int pw = 1;
-          for (int t = lane + 1; t < b; ++t) pw *= q;
-          contrib = dg * pw;
+          for (int i = 0; i < n; ++i) dg += (int)Ml[i * b + t] * (int)kl[i];
+          jl = jl * q + dg % q;
         }
-        const int jl = __reduce_add_sync(0xffffffffu, contrib);
         c2<T>* Ul = reinterpret_cast<c2<T>*>(plan.U) + job->off_U + (int64_t)l * RP * B + jl;
         const int8_t* Dl = plan.i8 + job->off_D + (int64_t)l * RP * n;
-        for (int r = lane; r < RP; r += 32) {
-          int ph = 0;
-          for (int i = 0; i < n; ++i) ph += (int)Dl[(int64_t)r * n + i] * (int)sk[wib][i];
-          const double2 w = root(plan.roots, q, ph % q);
-          const double dx = rho.x * w.x - rho.y * w.y;
-          const double dy = rho.x * w.y + rho.y * w.x;
-          T* p = reinterpret_cast<T*>(Ul + (int64_t)r * B);
-          atomicAdd(p, (T)(-dx));
-          atomicAdd(p + 1, (T)(-dy));
-        }
-        if (lane == 0) {  // queue the changed bin for the next scan (once per iteration)
-          const int lb = l * B + jl;
-          if (atomicExch(plan.bin_stamp + job->off_bin + lb, iter) != iter) {
-            const int pos = atomicAdd(&ctl->n_dirty[parity], 1);
-            list[pos] = lb;
+        if (sizeof(T) == 4) {
+          const float rx = (float)rho.x, ry = (float)rho.y;
+          for (int r = 0; r < RP; ++r) {
+            const double2 w = root(plan.roots, q, row_phase(Dl + (int64_t)r * n, kl, n, words_ok, q));
+            const float wx = (float)w.x, wy = (float)w.y;
+            sub_entry(Ul + (int64_t)r * B, rx * wx - ry * wy, rx * wy + ry * wx);
+          }
+        } else {
+          for (int r = 0; r < RP; ++r) {
+            const double2 w = root(plan.roots, q, row_phase(Dl + (int64_t)r * n, kl, n, words_ok, q));
+            sub_entry(Ul + (int64_t)r * B, rho.x * w.x - rho.y * w.y, rho.x * w.y + rho.y * w.x);
           }
         }
+        lb = l * B + jl;
+        fresh = atomicExch(plan.bin_stamp + job->off_bin + lb, iter) != iter;
       }
-      __syncwarp();
+      const int pos = warp_append(fresh, jid, &ctl->n_dirty[parity]);  // once per bin per iteration
+      if (fresh) list[pos] = lb;
     }
   }
 }
 
-__global__ void iter_end_kernel(qsft_plan plan) {
-  if (__ldcg(plan.done_count) >= plan.njobs) return;
-  const int jid = blockIdx.x * blockDim.x + threadIdx.x;
-  if (jid >= plan.njobs) return;
-  qsft_ctrl* ctl = plan.ctrl + jid;
-  const qsft_job* job = plan.jobs + jid;
-  if (ctl->done) return;
-  const int it = ctl->iter + 1;
-  ctl->iter = it;
-  ctl->num_peeling += ctl->n_unique;
-  if (ctl->n_multi == 0 || ctl->n_single == 0 || it >= job->max_iter || ctl->num_peeling >= job->peeling_max ||
-      ctl->err != 0) {
-    ctl->done = 1;
-    atomicAdd(plan.done_count, 1);
+// Per job: iteration count, cumulative peel count and the loop's stopping
+// rules (qsft/qsft.py:151, 204-205).  One block walks all jobs; when the
+// iteration loop runs as a CUDA-graph WHILE node (set_cond), thread 0 then
+// sets the loop condition: some job still running and fewer than max_iter
+// iterations done.
+__global__ void __launch_bounds__(256) iter_end_kernel(qsft_plan plan, cudaGraphConditionalHandle cond, int set_cond,
+                                                       int max_iter) {
+  __shared__ int s_iter;
+  if (threadIdx.x == 0) s_iter = 0;
+  __syncthreads();
+  if (__ldcg(plan.done_count) < plan.njobs) {
+    for (int jid = threadIdx.x; jid < plan.njobs; jid += blockDim.x) {
+      qsft_ctrl* ctl = plan.ctrl + jid;
+      const qsft_job* job = plan.jobs + jid;
+      if (ctl->done) continue;
+      const int it = ctl->iter + 1;
+      ctl->iter = it;
+      atomicMax(&s_iter, it);
+      ctl->num_peeling += ctl->n_unique;
+      if (ctl->n_multi == 0 || ctl->n_single == 0 || it >= job->max_iter || ctl->num_peeling >= job->peeling_max ||
+          ctl->err != 0) {
+        ctl->done = 1;
+        atomicAdd(plan.done_count, 1);
+      }
+      ctl->n_single = 0;
+      ctl->n_unique = 0;
+      ctl->n_cand = 0;
+      ctl->n_dirty[(it - 1) & 1] = 0;  // consumed by this iteration's scan
+    }
   }
-  ctl->n_single = 0;
-  ctl->n_unique = 0;
-  ctl->n_cand = 0;
-  ctl->n_dirty[(it - 1) & 1] = 0;  // consumed by this iteration's scan
+  __syncthreads();
+  if (set_cond && threadIdx.x == 0)
+    cudaGraphSetConditional(cond, (__ldcg(plan.done_count) < plan.njobs && s_iter < max_iter) ? 1u : 0u);
 }
 
 template <typename T>
-static int iteration(const qsft_plan* plan, int first, cudaStream_t st) {
+static int iteration(const qsft_plan* plan, int first, cudaStream_t st, cudaGraphConditionalHandle cond = 0,
+                     int set_cond = 0, int max_iter = 0) {
   if (first) {
     const int64_t grid = (plan->total_bins + SCAN_THREADS - 1) / SCAN_THREADS;
     if (grid > 0x7fffffffLL) return QSFT_ERR_TOO_LARGE;
@@ -530,16 +616,79 @@ static int iteration(const qsft_plan* plan, int first, cudaStream_t st) {
   QSFT_CUDA_CHECK_LAUNCH();
   decode_kernel<T><<<LIST_BLOCKS, WARPS_PER_BLOCK * 32, 0, st>>>(*plan);
   QSFT_CUDA_CHECK_LAUNCH();
-  peel_kernel<T><<<LIST_BLOCKS, WARPS_PER_BLOCK * 32, 0, st>>>(*plan);
+  record_kernel<<<LIST_BLOCKS, SCAN_THREADS, 0, st>>>(*plan);
   QSFT_CUDA_CHECK_LAUNCH();
-  iter_end_kernel<<<(plan->njobs + 127) / 128, 128, 0, st>>>(*plan);
+  peel_kernel<T><<<LIST_BLOCKS, SCAN_THREADS, 0, st>>>(*plan);
+  QSFT_CUDA_CHECK_LAUNCH();
+  iter_end_kernel<<<1, 256, 0, st>>>(*plan, cond, set_cond, max_iter);
   QSFT_CUDA_CHECK_LAUNCH();
   return QSFT_OK;
 }
 
+// The body of the WHILE node: iterations 2.. as kernel nodes of `body`.
+template <typename T>
+static int add_body(const qsft_plan* plan, cudaGraph_t body, cudaGraphConditionalHandle cond, int max_iter) {
+  qsft_plan pl = *plan;
+  int set = 1, mi = max_iter;
+  void* a1[] = {&pl};
+  void* a5[] = {&pl, &cond, &set, &mi};
+  struct K {
+    void* f;
+    unsigned grid, block;
+    void** args;
+  } ks[] = {{(void*)scan_dirty_kernel<T>, LIST_BLOCKS, SCAN_THREADS, a1},
+            {(void*)decode_kernel<T>, LIST_BLOCKS, WARPS_PER_BLOCK * 32, a1},
+            {(void*)record_kernel, LIST_BLOCKS, SCAN_THREADS, a1},
+            {(void*)peel_kernel<T>, LIST_BLOCKS, SCAN_THREADS, a1},
+            {(void*)iter_end_kernel, 1, 256, a5}};
+  cudaGraphNode_t prev = nullptr;
+  for (const K& k : ks) {
+    cudaKernelNodeParams kp = {};
+    kp.func = k.f;
+    kp.gridDim = dim3(k.grid);
+    kp.blockDim = dim3(k.block);
+    kp.kernelParams = k.args;
+    cudaGraphNode_t node;
+    if (cudaGraphAddKernelNode(&node, body, prev ? &prev : nullptr, prev ? 1 : 0, &kp) != cudaSuccess)
+      return QSFT_ERR_CUDA;
+    count_launch();
+    prev = node;
+  }
+  return QSFT_OK;
+}
+
+// Inside a stream capture: iteration 1 on the stream, then one WHILE node
+// whose body runs further iterations only while some job is still in its
+// loop -- finished batches cost no launches.
+template <typename T>
+static int run_graph(const qsft_plan* plan, int max_iter, cudaStream_t st) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess) return QSFT_ERR_CUDA;
+  cudaGraphConditionalHandle cond;
+  if (cudaGraphConditionalHandleCreate(&cond, g, 0, cudaGraphCondAssignDefault) != cudaSuccess) return QSFT_ERR_CUDA;
+  int rc = iteration<T>(plan, 1, st, cond, 1, max_iter);
+  if (rc != QSFT_OK || max_iter <= 1) return rc;
+  if (cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd) != cudaSuccess) return QSFT_ERR_CUDA;
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = cond;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (cudaGraphAddNode(&node, g, deps, nullptr, nd, &np) != cudaSuccess) return QSFT_ERR_CUDA;
+  rc = add_body<T>(plan, np.conditional.phGraph_out[0], cond, max_iter);
+  if (rc != QSFT_OK) return rc;
+  if (cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies) != cudaSuccess)
+    return QSFT_ERR_CUDA;
+  return QSFT_OK;
+}
+
 static int check_plan(const qsft_plan* p) {
-  if (!p || p->njobs <= 0 || !p->jobs || !p->bin_prefix || !p->i8 || !p->U || !p->kbuf || !p->rho ||
-      !p->tab_key || !p->tab_best || !p->uniq || !p->ball_tab || !p->ball_k || !p->ball_sum || !p->ball_cnt ||
+  if (!p || p->njobs <= 0 || !p->jobs || !p->bin_prefix || !p->i8 || !p->U || !p->kbuf || !p->rho || !p->ball_best ||
+      !p->uniq || !p->ball_tab || !p->ball_k || !p->ball_sum || !p->ball_cnt ||
       !p->ctrl || !p->roots || !p->bin_status || !p->bin_stamp || !p->dirty || !p->cand || !p->done_count)
     return QSFT_ERR_ARG;
   if (p->kstride < 16 || (p->kstride & 15) || p->kstride > QSFT_MAX_N + 16) return QSFT_ERR_ARG;
@@ -558,9 +707,8 @@ extern "C" int qsft_peel_init(const qsft_plan* plan, qsft_stream_t stream) {
   if (rc != QSFT_OK) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   if (cudaMemsetAsync(plan->ctrl, 0, sizeof(qsft_ctrl) * plan->njobs, st) != cudaSuccess ||
-      cudaMemsetAsync(plan->tab_key, 0, sizeof(int64_t) * plan->total_slots, st) != cudaSuccess ||
-      cudaMemsetAsync(plan->tab_best, 0, sizeof(int64_t) * plan->total_slots, st) != cudaSuccess ||
-      cudaMemsetAsync(plan->ball_tab, 0, sizeof(int32_t) * plan->total_slots, st) != cudaSuccess ||
+      cudaMemsetAsync(plan->ball_tab, 0, sizeof(int64_t) * plan->total_slots, st) != cudaSuccess ||
+      cudaMemsetAsync(plan->ball_best, 0, sizeof(int64_t) * plan->total_balls, st) != cudaSuccess ||
       cudaMemsetAsync(plan->ball_sum, 0, sizeof(double) * 2 * plan->total_balls, st) != cudaSuccess ||
       cudaMemsetAsync(plan->ball_cnt, 0, sizeof(int32_t) * plan->total_balls, st) != cudaSuccess ||
       cudaMemsetAsync(plan->bin_stamp, 0, sizeof(int32_t) * plan->total_bins, st) != cudaSuccess ||
@@ -578,9 +726,17 @@ extern "C" int qsft_peel_iteration(const qsft_plan* plan, int first, qsft_stream
 
 extern "C" int qsft_peel_run(const qsft_plan* plan, int max_iter, qsft_stream_t stream) {
   if (max_iter < 0) return QSFT_ERR_ARG;
-  for (int i = 0; i < max_iter; ++i) {
-    const int rc = qsft_peel_iteration(plan, i == 0, stream);
-    if (rc != QSFT_OK) return rc;
+  if (max_iter == 0) return QSFT_OK;
+  const int rc = check_plan(plan);
+  if (rc != QSFT_OK) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaStreamCaptureStatus cs;
+  if (cudaStreamIsCapturing(st, &cs) != cudaSuccess) return QSFT_ERR_CUDA;
+  if (cs == cudaStreamCaptureStatusActive)
+    return plan->prec == QSFT_F32 ? run_graph<float>(plan, max_iter, st) : run_graph<double>(plan, max_iter, st);
+  for (int i = 0; i < max_iter; ++i) {  // eager: finished jobs make the later launches no-ops
+    const int r = plan->prec == QSFT_F32 ? iteration<float>(plan, i == 0, st) : iteration<double>(plan, i == 0, st);
+    if (r != QSFT_OK) return r;
   }
   return QSFT_OK;
 }

@@ -218,12 +218,11 @@ class Batch:
         self.gf = up(self.gf_host, torch.int32)
         self.gwht_groups = {k: up(v, torch.int64) for k, v in self.gwht_rows_host.items()}
         self.roots = roots_table(dev)
-        self.kbuf = z(self.total_bins * self.kstride, torch.uint8)
         self.rho = z(self.total_bins * 2, torch.float64)
-        self.tab_key = z(self.total_slots, torch.int64)
-        self.tab_best = z(self.total_slots, torch.int64)
-        self.uniq = z(self.total_slots, torch.int32)
-        self.ball_tab = z(self.total_slots, torch.int32)
+        self.kbuf = z(self.total_bins * self.kstride, torch.uint8)
+        self.ball_tab = z(self.total_slots, torch.int64)
+        self.ball_best = z(self.total_balls, torch.int64)
+        self.uniq = z(self.total_balls, torch.int32)
         self.ball_k = z(self.total_balls * self.kstride, torch.uint8)
         self.ball_sum = z(self.total_balls * 2, torch.float64)
         self.ball_cnt = z(self.total_balls, torch.int32)
@@ -258,8 +257,8 @@ class Batch:
         ptr = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
         p.jobs, p.eval_prefix, p.bin_prefix = ptr(self.jobs_dev), ptr(self.eval_prefix), ptr(self.bin_prefix)
         p.i8, p.A, p.U, p.gf_tables, p.roots = ptr(self.i8), ptr(self.A), ptr(self.U), ptr(self.gf), ptr(self.roots)
-        p.kbuf, p.rho, p.tab_key, p.tab_best = ptr(self.kbuf), ptr(self.rho), ptr(self.tab_key), ptr(self.tab_best)
-        p.uniq, p.ball_tab, p.ball_k = ptr(self.uniq), ptr(self.ball_tab), ptr(self.ball_k)
+        p.kbuf, p.rho, p.ball_tab, p.ball_best = ptr(self.kbuf), ptr(self.rho), ptr(self.ball_tab), ptr(self.ball_best)
+        p.uniq, p.ball_k = ptr(self.uniq), ptr(self.ball_k)
         p.ball_sum, p.ball_cnt, p.ctrl = ptr(self.ball_sum), ptr(self.ball_cnt), ptr(self.ctrl)
         p.bin_status, p.bin_stamp = ptr(self.bin_status), ptr(self.bin_stamp)
         p.dirty, p.cand = ptr(self.dirty), ptr(self.cand)
@@ -389,6 +388,14 @@ class Batch:
         self.graph_launches = self.lib.qsft_launch_count() - l0
         self.graph = g
         return g
+
+    def launches_per_run(self, ctrl=None):
+        """Library kernels one graph replay executed: the captured launches, with
+        the peeling loop's body (captured once) counted once per iteration
+        after the first that the jobs actually ran (read from the control records)."""
+        ctrl = self.ctrl_host() if ctrl is None else ctrl
+        extra = max(max(int(c.iter) for c in ctrl) - 2, -1)
+        return self.graph_launches + _lib.PEEL_LAUNCHES_PER_ITER * extra
 
     def run(self):
         """One step: graph replay when captured, else direct launches."""
