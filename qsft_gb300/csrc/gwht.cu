@@ -143,6 +143,156 @@ __global__ void __launch_bounds__(512) gwht_pass_kernel(c2<T>* __restrict__ data
   }
 }
 
+// ---------------------------------------------------------------- row path
+// q in {2, 4}, whole row in shared memory (FP32 rows up to 16384 values, FP64
+// up to 8192).  A persistent CTA of B/16 threads transforms whole rows: every
+// pass gives each thread 16 elements -- 16/G groups of G = q^m elements along
+// m consecutive digits -- and applies the q-point DFT along each digit in
+// registers.  The first pass reads global memory and the last one writes it;
+// passes in between go through shared memory, padded by one value every 16 so
+// that every access pattern needs only the minimum of bank wavefronts.  While a row
+// is transformed, the row after next is prefetched into L2.
+__device__ __forceinline__ int pad16(int e) { return e + (e >> 4); }
+
+template <typename V, int Q, int G>
+__device__ __forceinline__ void groups_dft(V (&x)[16]) {
+#pragma unroll
+  for (int st = G / Q; st >= 1; st /= Q) {  // stride of each digit of the group
+#pragma unroll
+    for (int k = 0; k < 16 / G; ++k) {
+#pragma unroll
+      for (int m = 0; m < G; ++m) {
+        if ((m / st) % Q) continue;  // m = first element of a DFT along this digit
+        V v[Q];
+#pragma unroll
+        for (int r = 0; r < Q; ++r) v[r] = x[k * G + m + r * st];
+        dft_small<V, Q>(v, nullptr);
+#pragma unroll
+        for (int r = 0; r < Q; ++r) x[k * G + m + r * st] = v[r];
+      }
+    }
+  }
+}
+
+// one pass over digits [d0, d0 + m) with G = q^m; slo = stride of the lowest of them
+template <typename T, int Q, int G>
+__device__ __forceinline__ void row_pass(c2<T> (&x)[16], int t, int B, int slo, int mode, const c2<T>* src,
+                                         c2<T>* tile, c2<T>* dst, T scale) {
+  const int nthr = B >> 4;
+  int base[16 / G];
+#pragma unroll
+  for (int k = 0; k < 16 / G; ++k) {
+    const int gi = t + k * nthr;
+    base[k] = (gi % slo) + (gi / slo) * (slo * G);
+  }
+  // load: mode 0 from global (first pass), else from the padded tile
+#pragma unroll
+  for (int k = 0; k < 16 / G; ++k)
+#pragma unroll
+    for (int m = 0; m < G; ++m) {
+      const int e = base[k] + m * slo;
+      x[k * G + m] = mode == 0 ? src[e] : tile[pad16(e)];
+    }
+  groups_dft<c2<T>, Q, G>(x);
+  // store: mode 2 to global (last pass, scaled), else to the tile
+#pragma unroll
+  for (int k = 0; k < 16 / G; ++k)
+#pragma unroll
+    for (int m = 0; m < G; ++m) {
+      const int e = base[k] + m * slo;
+      if (mode == 2) {
+        c2<T> v = x[k * G + m];
+        v.x *= scale;
+        v.y *= scale;
+        dst[e] = v;
+      } else {
+        tile[pad16(e)] = x[k * G + m];
+      }
+    }
+}
+
+template <typename T, int Q>
+__device__ __forceinline__ void row_pass_any(int nd, c2<T> (&v)[16], int t, int B, int slo, int mode, c2<T>* x,
+                                             c2<T>* tile, T scale) {
+  if constexpr (Q == 4) {
+    if (nd == 2) row_pass<T, 4, 16>(v, t, B, slo, mode, x, tile, x, scale);
+    else row_pass<T, 4, 4>(v, t, B, slo, mode, x, tile, x, scale);
+  } else {
+    if (nd == 4) row_pass<T, 2, 16>(v, t, B, slo, mode, x, tile, x, scale);
+    else if (nd == 3) row_pass<T, 2, 8>(v, t, B, slo, mode, x, tile, x, scale);
+    else if (nd == 2) row_pass<T, 2, 4>(v, t, B, slo, mode, x, tile, x, scale);
+    else row_pass<T, 2, 2>(v, t, B, slo, mode, x, tile, x, scale);
+  }
+}
+
+// rows of B = q^b >= 256 values: at least two passes (first from, last to global);
+// the top and the lowest DPP digits are disjoint full groups
+template <typename T, int Q>
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 1024 : 512) gwht_row_kernel(c2<T>* __restrict__ data, const int64_t* __restrict__ row_off,
+                                                        int64_t nrows, int b) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  c2<T>* tile = reinterpret_cast<c2<T>*>(smem);
+  constexpr int LQ = Q == 4 ? 2 : 1;  // bits per digit
+  constexpr int DPP = 4 / LQ;         // digits per full pass (16 elements)
+  const int B = 1 << (LQ * b);
+  const int t = threadIdx.x;
+  const T scale = (T)1 / (T)B;        // exact: B is a power of two
+  const int npass = (b + DPP - 1) / DPP;
+  for (int64_t row = blockIdx.x; row < nrows; row += gridDim.x) {
+    c2<T>* x = data + __ldg(row_off + row);
+    if (t == 0 && row + 2 * (int64_t)gridDim.x < nrows) {  // the row after next, into L2
+      const c2<T>* nx = data + __ldg(row_off + row + 2 * (int64_t)gridDim.x);
+      const uint32_t bytes = (uint32_t)B * (uint32_t)sizeof(c2<T>);
+      if (((reinterpret_cast<uintptr_t>(nx) | bytes) & 15) == 0)
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(nx), "r"(bytes) : "memory");
+    }
+    c2<T> v[16];
+    // pass order (the digit axes are independent): the top DPP digits first
+    // (global reads, consecutive lanes on consecutive values), the lowest DPP
+    // next, then the groups in between from low to high -- the last pass,
+    // which writes global memory, is the one just below the top digits and
+    // its values are at least 16 apart, so lanes still cover whole lines
+    for (int p = 0; p < npass; ++p) {
+      int d0, d1;
+      if (p == 0) {
+        d0 = 0;
+        d1 = DPP;
+      } else {
+        d1 = b - (p - 1) * DPP;
+        d0 = d1 - DPP > DPP ? d1 - DPP : DPP;
+      }
+      const int mode = p == 0 ? 0 : (p == npass - 1 ? 2 : 1);
+      row_pass_any<T, Q>(d1 - d0, v, t, B, 1 << (LQ * (b - d1)), mode, x, tile, scale);
+      __syncthreads();
+    }
+  }
+}
+
+template <typename T, int Q>
+static int launch_row(c2<T>* data, const int64_t* row_off, int64_t nrows, int b, cudaStream_t st) {
+  const int LQ = Q == 4 ? 2 : 1;
+  const int B = 1 << (LQ * b);
+  const int threads = B / 16;
+  const int sm = (B + B / 16) * (int)sizeof(c2<T>);
+  auto kern = gwht_row_kernel<T, Q>;
+  if (!ensure_smem((const void*)kern, sm)) return QSFT_ERR_CUDA;
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+      return QSFT_ERR_CUDA;
+  }
+  // resident CTAs per SM: shared memory and threads
+  int per = (227 * 1024) / (sm + 1024);
+  if (per > 2048 / threads) per = 2048 / threads;
+  if (per < 1) per = 1;
+  int64_t grid = (int64_t)sms * per;
+  if (grid > nrows) grid = nrows;
+  kern<<<(unsigned)grid, threads, sm, st>>>(data, row_off, nrows, b);
+  QSFT_CUDA_CHECK_LAUNCH();
+  return QSFT_OK;
+}
+
 // ---------------------------------------------------------------- cluster path
 // A row of B = q^b values is split over a cluster of CS = q^k CTAs (CTA j holds
 // elements [j*Bp, (j+1)*Bp), Bp = B/CS).  Axes 0..k-1 span the CTAs: their
@@ -389,6 +539,12 @@ static int run_gwht(int q, int b, void* data, const int64_t* row_off, int64_t nr
   if (np <= 0) return QSFT_ERR_TOO_LARGE;
   c2<T>* d = reinterpret_cast<c2<T>*>(data);
   const T div = (T)ipow(q, b);
+  if ((q == 2 || q == 4)) {
+    const int bits = (q == 4 ? 2 : 1) * b;
+    const int maxbits = sizeof(T) == 4 ? 14 : 13;  // whole row in shared memory
+    if (bits >= 8 && bits <= maxbits)
+      return q == 4 ? launch_row<T, 4>(d, row_off, nrows, b, st) : launch_row<T, 2>(d, row_off, nrows, b, st);
+  }
   int k = 0;
   const int CS = cluster_split(q, b, es, &k);
   if (CS > 0) {
