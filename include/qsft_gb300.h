@@ -169,10 +169,10 @@ typedef struct qsft_plan {
   int64_t total_gm_prep;       /* blocks of the operand kernel                      */
   int64_t gm_ws_bytes;
   int32_t gm_mt;               /* 128-row MMA tiles per CTA (1, 2 or 4)             */
-  int32_t gm_kps;              /* K entries per support vector: 4 when every q is 2
-                                * or 4 (exact FP16 characters), else 8             */
+  int32_t gm_kps;              /* K entries per support vector: 2 when every q is 2
+                                * or 4 (exact FP16 characters), else 4             */
   int32_t gm_nw;               /* 32-bit words of packed b-digit vectors (1, 2, 4)  */
-  int32_t gm_npmax;            /* largest N extent: 2*R*P rounded up to 16          */
+  int32_t gm_npmax;            /* largest N extent: 4*min(R*P, 64) rounded up to 16 */
   int32_t gm_jt_bytes;         /* shared-memory bytes of the largest j table        */
   int32_t gm_pad_;
 } qsft_plan;
@@ -219,7 +219,7 @@ int qsft_eval_cosets_tc(const qsft_plan* plan, qsft_stream_t stream);
  *               = (W C)[l][rp],
  * W the q^b x S character matrix of the j_s (exact in FP16 for q in {2, 4};
  * hi + lo FP16 halves otherwise) and C the S x R*P coefficient matrix (hi + lo
- * FP16 halves of a per-job power-of-two scaling).  An operand kernel builds C
+ * FP16 halves of a per-job power-of-two scaling, as separate N columns).  An operand kernel builds C
  * and the j_s into gm_ws; the GEMM kernel generates W tiles in shared memory
  * and runs tcgen05.mma kind::f16 into tensor memory.  U needs no zeroing.
  * Needs the plan's gm_* fields from qsft_gemm_layout.
@@ -231,7 +231,7 @@ int qsft_eval_cosets_gemm(const qsft_plan* plan, qsft_stream_t stream);
  * total_gm_work, total_gm_prep, gm_ws_bytes and index_host[3*njobs+2] (to be
  * uploaded to plan->gm_index).  A plan->gm_mt of 1 or 2 on entry caps the
  * 128-row tiles per CTA (default 4).  QSFT_ERR_TOO_LARGE when a job is outside the
- * kernel's limits (q > 32, b > 16, 2*R*P > 256, S > 8192): use
+ * kernel's limits (q > 32, b > 16, R*P > 128, S > 8192): use
  * qsft_eval_cosets_tc for such batches.
  */
 int qsft_gemm_layout(const qsft_job* jobs_host, int njobs, qsft_plan* plan, int64_t* index_host);

@@ -18,18 +18,23 @@
 // tensor core multiplies exactly and accumulates in FP32.
 //
 // Real GEMM layout.  Complex products become real ones over K entries per
-// support vector (KPS):
-//   KPS = 4 (q in {2, 4}):  A[l][4s..4s+3] = [Wr, Wi, Wr, Wi]
-//     B[4s..4s+3][2rp]   = [Chr, -Chi, Clr, -Cli]   (real part of W C)
-//     B[4s..4s+3][2rp+1] = [Chi,  Chr, Cli,  Clr]   (imaginary part)
-//   KPS = 8:                A[l][8s..8s+7] = [Whr, Whi, Whr, Whi, Wlr, Wli, Wlr, Wli]
-//     B rows repeat the four KPS = 4 rows twice.
-// N = 2*R*P rounded up to 16 (<= 256).  An operand kernel writes B (and the
+// support vector (KPS) and four N columns per delay row, (re, im) x (hi, lo)
+// of the coefficient:
+//   KPS = 2 (q in {2, 4}):  A[l][2s..2s+1] = [Wr, Wi]
+//     B[2s..2s+1][4rp + 0, 1] = [Chr, -Chi], [Clr, -Cli]   (real part of W C)
+//     B[2s..2s+1][4rp + 2, 3] = [Chi,  Chr], [Cli,  Clr]   (imaginary part)
+//   KPS = 4:                A[l][4s..4s+3] = [Whr, Whi, Wlr, Wli]
+//     B rows repeat the two KPS = 2 rows for the W_lo entries.
+// The epilogue adds the hi and lo columns.  Putting the C halves on N rather
+// than K keeps K at 2 (or 4) entries per support vector, so each MMA reads
+// fewer operand bytes from shared memory per multiply-add: that read rate,
+// not the multiplier array, bounds a single-CTA MMA with N <= 256.  Delay rows
+// go in chunks of up to 64 (N <= 256).  An operand kernel writes B (and the
 // packed j_s digits) into a workspace in the exact shared-memory image of each
-// 64-entry K chunk (128-byte-swizzled K-major rows), so the GEMM kernel streams it with one bulk copy per
-// stage.  The GEMM kernel generates A in shared memory from the row's digits
-// (two dp4a per support vector for b <= 8) and issues tcgen05.mma kind::f16
-// (M = 128, N, K = 16) into tensor memory.
+// 64-entry K chunk (128-byte-swizzled K-major rows), so the GEMM kernel streams
+// it with one bulk copy per stage.  The GEMM kernel generates A in shared memory
+// from the row's digits (two dp4a per support vector for b <= 8) and issues
+// tcgen05.mma kind::f16 (M = 128, N, K = 16) into tensor memory.
 //
 // CTA: MT tiles of 128 rows (one producer thread per row, MT*128 threads),
 // one MMA-issuing warp and one bulk-copy warp.  A chunks and B chunks live in
@@ -55,19 +60,27 @@ constexpr int PREP_S = 32;                 // support vectors per operand block
 constexpr int REGION_HDR = 256;            // per-job header (inverse scale)
 constexpr int MAX_SMEM = 227 * 1024;
 
+constexpr int RPC_MAX = 64;                // delay rows per N chunk (N = 4 columns each)
+
 struct Geo {
-  int NP, S_pad, nK;
-  uint32_t CB;       // bytes of one B chunk (NP x KC FP16)
-  int64_t region_c;  // bytes per group: nK chunks + j table, 256-aligned
+  int RPC, nch;      // delay rows per chunk, chunks
+  int NP;            // N extent: 4*RPC rounded up to 16
+  int S_pad, nK;     // support vectors padded to whole stages, K chunks
+  uint32_t CB;       // bytes of one B chunk image (NP x KC FP16)
+  int64_t jt_bytes;  // j table of a group, 256-aligned
+  int64_t region_c;  // bytes per group: j table + nch x nK B chunks
 };
 __host__ __device__ inline Geo geo(int RP, int S, int kps, int nw) {
   Geo g;
-  g.NP = (2 * RP + 15) / 16 * 16;
+  g.RPC = RP < RPC_MAX ? RP : RPC_MAX;
+  g.nch = (RP + g.RPC - 1) / g.RPC;
+  g.NP = (4 * g.RPC + 15) / 16 * 16;
   const int spc = KC / kps;
   g.S_pad = (S + spc - 1) / spc * spc;
   g.nK = g.S_pad * kps / KC;
   g.CB = (uint32_t)g.NP * KC * 2;
-  g.region_c = ((int64_t)g.nK * g.CB + (int64_t)g.S_pad * nw * 4 + 255) / 256 * 256;
+  g.jt_bytes = ((int64_t)g.S_pad * nw * 4 + 255) / 256 * 256;
+  g.region_c = g.jt_bytes + (int64_t)g.nch * g.nK * g.CB;
   return g;
 }
 __host__ __device__ inline int64_t region_bytes(const Geo& g, int C) { return REGION_HDR + (int64_t)C * g.region_c; }
@@ -155,7 +168,7 @@ __global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
   const float sc = ldexpf(1.0f, 14 - ex);
 
   // j table
-  uint32_t* jtab = reinterpret_cast<uint32_t*>(rc + (int64_t)g.nK * g.CB);
+  uint32_t* jtab = reinterpret_cast<uint32_t*>(rc);
   for (int e = tid; e < (s_hi - s_lo) * NW; e += blockDim.x) {
     const int sl = e / NW, wi = e % NW;
     uint32_t word = 0;
@@ -166,28 +179,29 @@ __global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
         int acc = 0;
         for (int i = 0; i < n; ++i) acc += (int)M[i * b + t] * (int)sK[sl * n + i];
         uint32_t v = (uint32_t)(acc % q);
-        if (KPS == 4 && q == 2) v *= 2;
+        if (KPS == 2 && q == 2) v *= 2;
         word |= v << (8 * k);
       }
     }
     jtab[(int64_t)(s_lo + sl) * NW + wi] = word;
   }
 
-  // B entries: (support vector, delay row) items write the row's two columns
-  auto dst = [&](int s, int nn) {
+  // B entries: (support vector, delay row) items write the row's four columns
+  auto dst = [&](int s, int h, int nn) {
     const int k0 = KPS * s;
     const int kc = k0 / KC, kin = k0 % KC;
-    return rc + (int64_t)kc * g.CB + sw128(nn, kin);
+    return rc + g.jt_bytes + ((int64_t)h * g.nK + kc) * g.CB + sw128(nn, kin);
   };
-  auto put = [&](unsigned char* p, uint32_t v0, uint32_t v1) {
-    if (KPS == 4)
-      *reinterpret_cast<uint2*>(p) = make_uint2(v0, v1);
+  auto put = [&](unsigned char* p, uint32_t v) {
+    if (KPS == 2)
+      *reinterpret_cast<uint32_t*>(p) = v;
     else
-      *reinterpret_cast<uint4*>(p) = make_uint4(v0, v1, v0, v1);
+      *reinterpret_cast<uint2*>(p) = make_uint2(v, v);
   };
   for (int e = tid; e < (s_hi - s_lo) * RP; e += blockDim.x) {
     const int sl = e / RP, rp = e % RP, s = s_lo + sl;
-    uint32_t re0 = 0, re1 = 0, im0 = 0, im1 = 0;
+    const int h = rp / g.RPC, nb = 4 * (rp - h * g.RPC);
+    uint32_t rh = 0, rl = 0, ih = 0, il = 0;
     if (sl < s_live) {
       int acc = 0;
       for (int i = 0; i < n; ++i) acc += (int)sD[rp * n + i] * (int)sK[sl * n + i];
@@ -197,17 +211,21 @@ __global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
       const float ci = (a.x * wr.y + a.y * wr.x) * sc;
       const __half hr = __float2half_rn(cr), hi = __float2half_rn(ci);
       const __half lr = __float2half_rn(cr - __half2float(hr)), li = __float2half_rn(ci - __half2float(hi));
-      re0 = h2_bits(hr, __hneg(hi));  // real-part column: [Chr, -Chi, Clr, -Cli]
-      re1 = h2_bits(lr, __hneg(li));
-      im0 = h2_bits(hi, hr);          // imaginary-part column: [Chi, Chr, Cli, Clr]
-      im1 = h2_bits(li, lr);
+      rh = h2_bits(hr, __hneg(hi));  // real-part columns: [Chr, -Chi], [Clr, -Cli]
+      rl = h2_bits(lr, __hneg(li));
+      ih = h2_bits(hi, hr);          // imaginary-part columns: [Chi, Chr], [Cli, Clr]
+      il = h2_bits(li, lr);
     }
-    put(dst(s, 2 * rp), re0, re1);
-    put(dst(s, 2 * rp + 1), im0, im1);
+    put(dst(s, h, nb + 0), rh);
+    put(dst(s, h, nb + 1), rl);
+    put(dst(s, h, nb + 2), ih);
+    put(dst(s, h, nb + 3), il);
   }
-  for (int e = tid; e < (s_hi - s_lo) * (g.NP - 2 * RP); e += blockDim.x) {  // padding columns
-    const int sl = e / (g.NP - 2 * RP), nn = 2 * RP + e % (g.NP - 2 * RP);
-    put(dst(s_lo + sl, nn), 0u, 0u);
+  // padding columns of every chunk (the last chunk may hold fewer delay rows)
+  for (int h = 0; h < g.nch; ++h) {
+    const int rows = min(g.RPC, RP - h * g.RPC), npad = g.NP - 4 * rows;
+    for (int e = tid; e < (s_hi - s_lo) * npad; e += blockDim.x)
+      put(dst(s_lo + e / npad, h, 4 * rows + e % npad), 0u);
   }
 }
 
@@ -226,7 +244,7 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 384);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 388);
   volatile int* n_con = reinterpret_cast<volatile int*>(smem + 392);
-  uint2* qtab = reinterpret_cast<uint2*>(smem + 512);  // KPS = 8: (hi, lo) half2 words of omega^m
+  uint2* qtab = reinterpret_cast<uint2*>(smem + 512);  // KPS = 4: (hi, lo) half2 words of omega^m
   uint32_t* jt = reinterpret_cast<uint32_t*>(smem + HDR);
   const int MT = plan.gm_mt;
   const uint32_t A_BYTES = (uint32_t)MT * A_TILE;
@@ -238,7 +256,7 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
   const int nprod = MT * TM;
   const int mma_warp = nprod / 32, load_warp = mma_warp + 1;
 
-  // ---- work item: (job, group, block of MT*128 rows)
+  // ---- work item: (job, group, chunk of delay rows, block of MT*128 rows)
   const int nj = plan.njobs;
   const int64_t* __restrict__ idx = plan.gm_index;
   const int64_t w = blockIdx.x;
@@ -248,12 +266,15 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
   const Geo g = geo(RP, S, KPS, NW);
   const int64_t rblocks = (B + nprod - 1) / nprod;
   const int64_t local = w - idx[j];
-  const int c = (int)(local / rblocks);
-  const int64_t row0 = (local - (int64_t)c * rblocks) * nprod;
+  const int ch = (int)(local / rblocks);  // (group, chunk)
+  const int c = ch / g.nch, h = ch - (ch / g.nch) * g.nch;
+  const int64_t row0 = (local - (int64_t)ch * rblocks) * nprod;
+  const int rp0 = h * g.RPC, nrp = min(g.RPC, RP - rp0);
   const unsigned char* region = reinterpret_cast<const unsigned char*>(plan.gm_ws) + idx[2 * (nj + 1) + j];
-  const unsigned char* gB = region + REGION_HDR + (int64_t)c * g.region_c;
-  const uint32_t* gJ = reinterpret_cast<const uint32_t*>(gB + (int64_t)g.nK * g.CB);
-  float2* __restrict__ U = reinterpret_cast<float2*>(plan.U) + job->off_U + (int64_t)c * RP * B;
+  const unsigned char* gc = region + REGION_HDR + (int64_t)c * g.region_c;
+  const uint32_t* gJ = reinterpret_cast<const uint32_t*>(gc);
+  const unsigned char* gB = gc + g.jt_bytes + (int64_t)h * g.nK * g.CB;
+  float2* __restrict__ U = reinterpret_cast<float2*>(plan.U) + job->off_U + ((int64_t)c * RP + rp0) * B;
 
   // ---- setup
   uint32_t ncols = 32;
@@ -277,7 +298,7 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
     *n_con = 0;
     fence_mbar_init();
   }
-  if (KPS == 8 && tid < q) {
+  if (KPS == 4 && tid < q) {
     const double* r = plan.roots + ((int64_t)q * 32 + tid) * 2;
     const float wr = (float)r[0], wi = (float)r[1];
     const __half hr = __float2half_rn(wr), hi = __float2half_rn(wi);
@@ -325,9 +346,24 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
       }
       unsigned char* ap = aring + st * A_BYTES + a_off;
       const int s0 = kc * (KC / KPS);
-      if constexpr (KPS == 4) {
-        // omega_4^m as half2 (re, im): high bytes from the tables 0x00BC003C (re)
-        // and 0xBC003C00 (im), low bytes zero
+      if constexpr (KPS == 2) {
+        // four support vectors per 16-byte chunk; omega_4^m as half2 (re, im):
+        // high bytes from the tables 0x00BC003C (re) and 0xBC003C00 (im), low bytes zero
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const uint32_t* jp = jt + (s0 + 4 * i) * NW;
+          uint32_t wv[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            uint32_t d = 0;
+#pragma unroll
+            for (int k = 0; k < NW; ++k) d = __dp4a(lw[k], jp[u * NW + k], d);
+            wv[u] = __byte_perm(0x00BC003Cu, 0xBC003C00u, 0x4101u + (d & 3u) * 0x1010u);
+          }
+          *reinterpret_cast<uint4*>(ap + ((i * 16) ^ sw)) = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+        }
+      } else {
+        // two support vectors per chunk: (hi, lo) half2 words of omega^m
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
           const uint32_t* jp = jt + (s0 + 2 * i) * NW;
@@ -337,19 +373,8 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
             d0 = __dp4a(lw[k], jp[k], d0);
             d1 = __dp4a(lw[k], jp[NW + k], d1);
           }
-          const uint32_t w0 = __byte_perm(0x00BC003Cu, 0xBC003C00u, 0x4101u + (d0 & 3u) * 0x1010u);
-          const uint32_t w1 = __byte_perm(0x00BC003Cu, 0xBC003C00u, 0x4101u + (d1 & 3u) * 0x1010u);
-          *reinterpret_cast<uint4*>(ap + ((i * 16) ^ sw)) = make_uint4(w0, w0, w1, w1);
-        }
-      } else {
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const uint32_t* jp = jt + (s0 + i) * NW;
-          uint32_t d = 0;
-#pragma unroll
-          for (int k = 0; k < NW; ++k) d = __dp4a(lw[k], jp[k], d);
-          const uint2 h = qtab[modq(d, mq)];
-          *reinterpret_cast<uint4*>(ap + ((i * 16) ^ sw)) = make_uint4(h.x, h.x, h.y, h.y);
+          const uint2 h0 = qtab[modq(d0, mq)], h1 = qtab[modq(d1, mq)];
+          *reinterpret_cast<uint4*>(ap + ((i * 16) ^ sw)) = make_uint4(h0.x, h0.y, h1.x, h1.y);
         }
       }
       fence_async_smem();
@@ -369,27 +394,27 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
       float2* __restrict__ ur = U + row;
       const float inv = *reinterpret_cast<const float*>(region);
       const int ng = g.NP / 16;
+      // 16 columns = 4 delay rows x (re hi, re lo, im hi, im lo)
+      auto emit = [&](const uint32_t(&r)[16], int cg) {
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const int rp = cg * 4 + i;
+          if (live && rp < nrp)
+            ur[(int64_t)rp * B] =
+                make_float2((__uint_as_float(r[4 * i]) + __uint_as_float(r[4 * i + 1])) * inv,
+                            (__uint_as_float(r[4 * i + 2]) + __uint_as_float(r[4 * i + 3])) * inv);
+        }
+      };
       uint32_t ra[16], rb[16];
       tmem_ld16(tb, ra);
       for (int cg = 0; cg < ng; cg += 2) {
         tmem_ld_wait_regs(ra);
         if (cg + 1 < ng) tmem_ld16(tb + (cg + 1) * 16, rb);
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int rp = cg * 8 + i;
-          if (live && rp < RP)
-            ur[(int64_t)rp * B] = make_float2(__uint_as_float(ra[2 * i]) * inv, __uint_as_float(ra[2 * i + 1]) * inv);
-        }
+        emit(ra, cg);
         if (cg + 1 < ng) {
           tmem_ld_wait_regs(rb);
           if (cg + 2 < ng) tmem_ld16(tb + (cg + 2) * 16, ra);
-#pragma unroll
-          for (int i = 0; i < 8; ++i) {
-            const int rp = (cg + 1) * 8 + i;
-            if (live && rp < RP)
-              ur[(int64_t)rp * B] =
-                  make_float2(__uint_as_float(rb[2 * i]) * inv, __uint_as_float(rb[2 * i + 1]) * inv);
-          }
+          emit(rb, cg + 1);
         }
       }
     } else if (lane == 0) {
@@ -500,20 +525,23 @@ using namespace qsft;
 
 extern "C" int qsft_gemm_layout(const qsft_job* jobs, int njobs, qsft_plan* plan, int64_t* index) {
   if (!jobs || njobs <= 0 || !plan || !index) return QSFT_ERR_ARG;
-  int kps = 4, maxb = 0, npmax = 16, jt = 0;
+  int kps = 2, maxb = 0, jt = 0;
   int64_t maxB = 1;
   for (int i = 0; i < njobs; ++i) {
     const qsft_job& jb = jobs[i];
     if (jb.q < 2 || jb.n < 1 || jb.b < 1 || jb.C < 1 || jb.R < 1 || jb.P < 1 || jb.S < 1) return QSFT_ERR_ARG;
-    if (jb.q > QSFT_MAX_Q || jb.b > 16 || 2 * jb.R * jb.P > 256 || jb.S > 8192 || jb.n > QSFT_MAX_N)
+    if (jb.q > QSFT_MAX_Q || jb.b > 16 || jb.R * jb.P > gm::PREP_MAXRP || jb.S > 8192 || jb.n > QSFT_MAX_N)
       return QSFT_ERR_TOO_LARGE;
-    if (jb.q != 2 && jb.q != 4) kps = 8;
+    if (jb.q != 2 && jb.q != 4) kps = 4;
     maxb = maxb > jb.b ? maxb : jb.b;
     maxB = maxB > jb.B ? maxB : jb.B;
-    const int np = (2 * jb.R * jb.P + 15) / 16 * 16;
-    npmax = npmax > np ? npmax : np;
   }
   const int nw = maxb <= 4 ? 1 : (maxb <= 8 ? 2 : 4);
+  int npmax = 16;
+  for (int i = 0; i < njobs; ++i) {
+    const gm::Geo g = gm::geo(jobs[i].R * jobs[i].P, jobs[i].S, kps, nw);
+    npmax = npmax > g.NP ? npmax : g.NP;
+  }
   int mt = (plan->gm_mt == 1 || plan->gm_mt == 2) ? plan->gm_mt : gm::MAX_MT;
   while (mt > 1 && (mt * npmax > 512 || (int64_t)(mt / 2) * gm::TM >= maxB)) mt /= 2;
   int64_t work = 0, prep = 0, off = 0;
@@ -523,7 +551,7 @@ extern "C" int qsft_gemm_layout(const qsft_job* jobs, int njobs, qsft_plan* plan
     const qsft_job& jb = jobs[i];
     const gm::Geo g = gm::geo(jb.R * jb.P, jb.S, kps, nw);
     const int64_t rows = (int64_t)mt * gm::TM;
-    work += (int64_t)jb.C * ((jb.B + rows - 1) / rows);
+    work += (int64_t)jb.C * g.nch * ((jb.B + rows - 1) / rows);
     prep += (int64_t)jb.C * ((g.S_pad + gm::PREP_S - 1) / gm::PREP_S);
     index[i + 1] = work;
     index[njobs + 2 + i] = prep;
@@ -556,10 +584,10 @@ extern "C" int qsft_eval_cosets_gemm(const qsft_plan* plan, qsft_stream_t stream
     return QSFT_ERR_ARG;
   if (plan->total_gm_work <= 0) return QSFT_OK;
   cudaStream_t st = (cudaStream_t)stream;
-  if (plan->gm_kps == 4) {
+  if (plan->gm_kps == 2) {
     if (plan->max_q > 4) return QSFT_ERR_ARG;
-    return gm::launch_nw<4>(plan, st);
+    return gm::launch_nw<2>(plan, st);
   }
-  if (plan->gm_kps == 8) return gm::launch_nw<8>(plan, st);
+  if (plan->gm_kps == 4) return gm::launch_nw<4>(plan, st);
   return QSFT_ERR_ARG;
 }
