@@ -55,7 +55,8 @@ constexpr int KC = 64;                     // K entries per stage: one 128-byte 
 constexpr int TM = 128;                    // rows per MMA tile
 constexpr int HDR = 1024;                  // barriers, TMEM slot, flags, root table
 constexpr int MAX_MT = 4;
-constexpr uint32_t A_TILE = TM * KC * 2;   // bytes of one tile's A chunk (16 KB)
+constexpr int A_COLS = KC / 2;             // TMEM columns of one tile's A chunk (two FP16 per column)
+constexpr int NA = 2;                      // A stages (in tensor memory)
 constexpr int PREP_S = 32;                 // support vectors per operand block
 constexpr int REGION_HDR = 256;            // per-job header (inverse scale)
 constexpr int MAX_SMEM = 227 * 1024;
@@ -230,27 +231,24 @@ __global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
 }
 
 // ---------------------------------------------------------------- GEMM
-constexpr int MAX_NA = 4;  // A stages
 constexpr int MAX_NB = 8;  // B stages (deeper: their bulk copies come from L2)
 
 template <int KPS, int NW>
-__global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_plan plan, int na, int nb) {
+__global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_plan plan, int nb) {
   extern __shared__ __align__(1024) unsigned char smem[];
   uint64_t* bfull = reinterpret_cast<uint64_t*>(smem);  // [MAX_NB]
   uint64_t* bempty = bfull + MAX_NB;                    // [MAX_NB]
-  uint64_t* afull = bempty + MAX_NB;                    // [MAX_NA]
-  uint64_t* aempty = afull + MAX_NA;                    // [MAX_NA]
-  uint64_t* accf = aempty + MAX_NA;
+  uint64_t* afull = bempty + MAX_NB;                    // [NA]
+  uint64_t* aempty = afull + NA;                        // [NA]
+  uint64_t* accf = aempty + NA;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 384);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 388);
   volatile int* n_con = reinterpret_cast<volatile int*>(smem + 392);
   uint2* qtab = reinterpret_cast<uint2*>(smem + 512);  // KPS = 4: (hi, lo) half2 words of omega^m
   uint32_t* jt = reinterpret_cast<uint32_t*>(smem + HDR);
   const int MT = plan.gm_mt;
-  const uint32_t A_BYTES = (uint32_t)MT * A_TILE;
   const uint32_t B_SLOT = (uint32_t)plan.gm_npmax * KC * 2;
-  unsigned char* aring = smem + HDR + plan.gm_jt_bytes;
-  unsigned char* bring = aring + na * A_BYTES;
+  unsigned char* bring = smem + HDR + plan.gm_jt_bytes;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nprod = MT * TM;
@@ -277,8 +275,10 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
   float2* __restrict__ U = reinterpret_cast<float2*>(plan.U) + job->off_U + ((int64_t)c * RP + rp0) * B;
 
   // ---- setup
+  // tensor memory: MT accumulators of NP columns, then NA stages of MT A tiles
+  const uint32_t acols = (uint32_t)(MT * g.NP + 31) / 32 * 32;
   uint32_t ncols = 32;
-  while (ncols < (uint32_t)(MT * g.NP)) ncols <<= 1;
+  while (ncols < acols + (uint32_t)(NA * MT * A_COLS)) ncols <<= 1;
   if (warp == mma_warp) {
     tmem_alloc(tmem_slot, ncols);
     tmem_relinquish();
@@ -288,13 +288,13 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
       mbar_init(&bfull[i], 1);
       mbar_init(&bempty[i], 1);
     }
-    for (int i = 0; i < MAX_NA; ++i) {
+    for (int i = 0; i < NA; ++i) {
       mbar_init(&afull[i], MT * 4);
       mbar_init(&aempty[i], 1);
     }
     mbar_init(accf, 1);
     // the swizzled layout needs 1024-byte aligned atoms
-    *abort_flag = ((smem_u32(aring) | smem_u32(bring)) & 1023u) ? 1 : 0;
+    *abort_flag = (smem_u32(bring) & 1023u) ? 1 : 0;
     *n_con = 0;
     fence_mbar_init();
   }
@@ -332,11 +332,12 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
       }
     }
     const ModQ mq = make_modq(q);
-    const uint32_t a_off = (uint32_t)t * A_TILE + (uint32_t)(tr >> 3) * 1024 + (uint32_t)(tr & 7) * 128;
-    const uint32_t sw = (uint32_t)(tr & 7) * 16;  // the row's chunk swizzle, as a byte XOR: sw128(tr, 8i)
+    // this warp's TMEM lanes (its 32 rows of tile t) and the tile's A columns
+    const uint32_t a_lane = tmem + ((uint32_t)(warp & 3) * 32 << 16) + acols + (uint32_t)t * A_COLS;
+    (void)tr;
     for (int kc = 0; kc < nK; ++kc) {
-      const int st = kc % na;
-      const uint32_t ph = (uint32_t)(kc / na) & 1;
+      const int st = kc % NA;
+      const uint32_t ph = (uint32_t)(kc / NA) & 1;
       int go = 1;
       if (lane == 0) go = !*abort_flag && mbar_wait(&aempty[st], ph ^ 1);
       go = __shfl_sync(~0u, go, 0);
@@ -344,8 +345,8 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
         if (lane == 0) *abort_flag = 1;
         break;
       }
-      unsigned char* ap = aring + st * A_BYTES + a_off;
       const int s0 = kc * (KC / KPS);
+      uint32_t av[32];  // the row's 64 FP16 entries of this stage, K order
       if constexpr (KPS == 2) {
         // four support vectors per 16-byte chunk; omega_4^m as half2 (re, im):
         // high bytes from the tables 0x00BC003C (re) and 0xBC003C00 (im), low bytes zero
@@ -360,7 +361,8 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
             for (int k = 0; k < NW; ++k) d = __dp4a(lw[k], jp[u * NW + k], d);
             wv[u] = __byte_perm(0x00BC003Cu, 0xBC003C00u, 0x4101u + (d & 3u) * 0x1010u);
           }
-          *reinterpret_cast<uint4*>(ap + ((i * 16) ^ sw)) = make_uint4(wv[0], wv[1], wv[2], wv[3]);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) av[4 * i + u] = wv[u];
         }
       } else {
         // two support vectors per chunk: (hi, lo) half2 words of omega^m
@@ -374,10 +376,15 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
             d1 = __dp4a(lw[k], jp[NW + k], d1);
           }
           const uint2 h0 = qtab[modq(d0, mq)], h1 = qtab[modq(d1, mq)];
-          *reinterpret_cast<uint4*>(ap + ((i * 16) ^ sw)) = make_uint4(h0.x, h0.y, h1.x, h1.y);
+          av[4 * i] = h0.x;
+          av[4 * i + 1] = h0.y;
+          av[4 * i + 2] = h1.x;
+          av[4 * i + 3] = h1.y;
         }
       }
-      fence_async_smem();
+      tmem_st32(a_lane + (uint32_t)(st * MT * A_COLS), av);
+      tmem_st_wait();
+      tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(&afull[st]);
     }
@@ -426,23 +433,24 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
     // so they are built once and offset.
     if (lane == 0) {
       const uint32_t idesc = tc::make_idesc(TM, g.NP);
-      const uint64_t a0 = desc_sw128(smem_u32(aring)), b0 = desc_sw128(smem_u32(bring));
+      const uint64_t b0 = desc_sw128(smem_u32(bring));
       int con = 0;
       for (int kc = 0; kc < nK; ++kc) {
-        const int sa = kc % na, sbi = kc % nb;
+        const int sa = kc % NA, sbi = kc % nb;
         if (*abort_flag) break;
-        if (!mbar_wait(&bfull[sbi], (uint32_t)(kc / nb) & 1) || !mbar_wait(&afull[sa], (uint32_t)(kc / na) & 1)) {
+        if (!mbar_wait(&bfull[sbi], (uint32_t)(kc / nb) & 1) || !mbar_wait(&afull[sa], (uint32_t)(kc / NA) & 1)) {
           *abort_flag = 1;
           break;
         }
         tc_fence_after();
-        const uint64_t ad = a0 + ((sa * A_BYTES) >> 4), bd = b0 + ((sbi * B_SLOT) >> 4);
+        const uint32_t ad = tmem + acols + (uint32_t)(sa * MT * A_COLS);
+        const uint64_t bd = b0 + ((sbi * B_SLOT) >> 4);
         for (int t = 0; t < MT; ++t) {
           const uint32_t dt = tmem + (uint32_t)(t * g.NP);
-          const uint64_t at = ad + ((t * A_TILE) >> 4);
+          const uint32_t at = ad + (uint32_t)(t * A_COLS);
 #pragma unroll
           for (int ks = 0; ks < KC / 16; ++ks)  // K = 16 is 32 bytes along the swizzled row
-            mma_f16(dt, at + ks * 2, bd + ks * 2, idesc, (kc | ks) > 0);
+            mma_f16_ts(dt, at + ks * 8, bd + ks * 2, idesc, (kc | ks) > 0);
         }
         mma_commit(&aempty[sa]);
         mma_commit(&bempty[sbi]);
@@ -482,28 +490,28 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
 }
 
 // stage counts for the shared-memory budget: 4 A + 8 B stages, B first trimmed to 4
-inline bool pick_stages(int mt, int npmax, int jt_bytes, int& na, int& nb, int& smem) {
-  const int fixed = HDR + jt_bytes, ab = mt * (int)A_TILE, bb = npmax * KC * 2;
-  for (na = MAX_NA; na >= 2; --na)
-    for (nb = MAX_NB; nb >= 4; --nb)
-      if (fixed + na * ab + nb * bb <= MAX_SMEM) {
-        smem = fixed + na * ab + nb * bb;
-        return true;
-      }
+// B stages for the shared-memory budget (A lives in tensor memory)
+inline bool pick_stages(int npmax, int jt_bytes, int& nb, int& smem) {
+  const int fixed = HDR + jt_bytes, bb = npmax * KC * 2;
+  for (nb = MAX_NB; nb >= 2; --nb)
+    if (fixed + nb * bb <= MAX_SMEM) {
+      smem = fixed + nb * bb;
+      return true;
+    }
   return false;
 }
 
 template <int KPS, int NW>
 static int launch(const qsft_plan* p, cudaStream_t st) {
-  int na, nb, smem;
-  if (!pick_stages(p->gm_mt, p->gm_npmax, p->gm_jt_bytes, na, nb, smem)) return QSFT_ERR_TOO_LARGE;
+  int nb, smem;
+  if (!pick_stages(p->gm_npmax, p->gm_jt_bytes, nb, smem)) return QSFT_ERR_TOO_LARGE;
   if (p->total_gm_prep > 0) {
     gemm_prep_kernel<KPS, NW><<<(unsigned)p->total_gm_prep, 256, 0, st>>>(*p);
     QSFT_CUDA_CHECK_LAUNCH();
   }
   auto kern = eval_gemm_kernel<KPS, NW>;
   if (!ensure_smem((const void*)kern, smem)) return QSFT_ERR_CUDA;
-  kern<<<(unsigned)p->total_gm_work, p->gm_mt * TM + 64, smem, st>>>(*p, na, nb);
+  kern<<<(unsigned)p->total_gm_work, p->gm_mt * TM + 64, smem, st>>>(*p, nb);
   QSFT_CUDA_CHECK_LAUNCH();
   return QSFT_OK;
 }
@@ -543,7 +551,9 @@ extern "C" int qsft_gemm_layout(const qsft_job* jobs, int njobs, qsft_plan* plan
     npmax = npmax > g.NP ? npmax : g.NP;
   }
   int mt = (plan->gm_mt == 1 || plan->gm_mt == 2) ? plan->gm_mt : gm::MAX_MT;
-  while (mt > 1 && (mt * npmax > 512 || (int64_t)(mt / 2) * gm::TM >= maxB)) mt /= 2;
+  // tensor memory: accumulators (32-column aligned) + NA stages of A tiles <= 512 columns
+  while (mt > 1 && ((mt * npmax + 31) / 32 * 32 + gm::NA * mt * gm::A_COLS > 512 || (int64_t)(mt / 2) * gm::TM >= maxB))
+    mt /= 2;
   int64_t work = 0, prep = 0, off = 0;
   index[0] = 0;
   index[njobs + 1] = 0;
@@ -560,8 +570,8 @@ extern "C" int qsft_gemm_layout(const qsft_job* jobs, int njobs, qsft_plan* plan
     const int jtb = (g.S_pad * nw * 4 + 1023) / 1024 * 1024;  // keeps the rings 1024-byte aligned
     jt = jt > jtb ? jt : jtb;
   }
-  int na, nb, smem;
-  if (!gm::pick_stages(mt, npmax, jt, na, nb, smem)) return QSFT_ERR_TOO_LARGE;
+  int nb, smem;
+  if (!gm::pick_stages(npmax, jt, nb, smem)) return QSFT_ERR_TOO_LARGE;
   if (work > 0x7fffffffLL || prep > 0x7fffffffLL) return QSFT_ERR_TOO_LARGE;
   plan->gm_mt = mt;
   plan->gm_kps = kps;
