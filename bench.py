@@ -198,11 +198,11 @@ def run_ours(args):
     batch = Batch([r.spec() for r in reqs], precision=args.precision, device=dev)
     stream = torch.cuda.current_stream()
     ev = {k: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for k in ("eval", "gwht", "noise", "peel", "collect")}
+          for k in ("eval", "gwht+noise", "peel", "collect")}
     acc = {k: 0.0 for k in ev}
 
-    phases = (("eval", batch.eval), ("gwht", batch.gwht), ("noise", batch.add_noise),
-              ("peel", batch.peel), ("collect", batch.collect_async))
+    phases = (("eval", batch.eval), ("gwht+noise", batch.gwht_noise), ("peel", batch.peel),
+              ("collect", batch.collect_async))
     phase_graphs = {}
 
     def step(timed):
@@ -270,7 +270,7 @@ def run_ours(args):
     b64 = Batch([reqs[0].spec()], precision="fp64", device=dev)
 
     def step64():
-        b64.eval(); b64.gwht(); b64.add_noise(); b64.peel(); b64.collect_async()
+        b64.eval(); b64.gwht_noise(); b64.peel(); b64.collect_async()
     for _ in range(2):
         step64()
     barrier()
@@ -309,7 +309,7 @@ def run_ours(args):
     bf16 = peaks.get("bf16_tflops", 1900.0)
     hbm = peaks.get("hbm_gbs", 6800.0)
     e_ms = phase_ms["eval"]
-    g_ms = phase_ms["gwht"]
+    g_ms = phase_ms["gwht+noise"]
     gwht_bytes = 2.0 * samples * 8 * J
     roofline = {"kernel": "eval_cosets_gemm (operand + GEMM kernels)", "bound": "tensor",
                 "achieved": eval_flops / (e_ms / 1e3) / 1e12,
@@ -317,7 +317,7 @@ def run_ours(args):
                 "peak_source": "measured" if "bf16_tflops" in peaks else "fallback",
                 "issued_tflops": None if issued is None else issued / (e_ms / 1e3) / 1e12}
     roofline["frac"] = roofline["achieved"] / roofline["peak"]
-    roof_gwht = {"kernel": "gwht", "bound": "hbm", "achieved": gwht_bytes / (g_ms / 1e3) / 1e9, "peak": hbm,
+    roof_gwht = {"kernel": "gwht_row (transform + bin noise, one read and one write)", "bound": "hbm", "achieved": gwht_bytes / (g_ms / 1e3) / 1e9, "peak": hbm,
                  "unit": "GB/s", "traffic": None, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
     roof_gwht["frac"] = roof_gwht["achieved"] / roof_gwht["peak"]
     line = {

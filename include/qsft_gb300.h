@@ -255,13 +255,25 @@ int qsft_eval_points(int prec, int q, int n, int S, const int8_t* X, int64_t npo
 int qsft_gwht(int prec, int q, int b, void* data, const int64_t* row_off, int64_t nrows,
               qsft_stream_t stream);
 
+/*
+ * qsft_gwht over rows of plan->U (row_off as for qsft_gwht) followed by the
+ * device bin noise of qsft_add_noise_philox for those rows, fused into the
+ * transform's last pass where the shape allows (q in {2, 4}): the bins are
+ * read and written once.  row_meta[2i], row_meta[2i+1] = the job of row i and
+ * the row's index within that job (c*R*P + r*P + p).  Jobs with noise_nu = 0
+ * get the plain transform.
+ */
+int qsft_gwht_noise(const qsft_plan* plan, int q, int b, const int64_t* row_off, const int32_t* row_meta,
+                    int64_t nrows, qsft_stream_t stream);
+
 /* ---- bin noise ---------------------------------------------------------- */
 /*
  * Replaces the bin-domain AWGN of SyntheticSubsampledSignal.get_MDU
  * (synthetic_signal.py:126-129): U += N(0, nu^2) + i N(0, nu^2) per entry,
  * nu = jobs[j].noise_nu, drawn from a counter-based Philox-4x32-10 stream keyed
- * by jobs[j].noise_seed (not numpy's stream: for reference-identical noise the
- * host draws it and adds it with qsft_add_bins).
+ * by jobs[j].noise_seed: draw row*half + e (half = ceil(q^b / 2)) gives entries
+ * e and e + half of the job's row `row` (not numpy's stream: for
+ * reference-identical noise the host draws it and adds it with qsft_add_bins).
  */
 int qsft_add_noise_philox(const qsft_plan* plan, qsft_stream_t stream);
 /* U[i] += X[i] for count complex values (host-drawn noise, uploaded) */

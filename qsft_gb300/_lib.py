@@ -29,7 +29,7 @@ PEEL_LAUNCHES_PER_ITER = 5   # QSFT_PEEL_LAUNCHES_PER_ITER
 SYMBOLS = [
     "qsft_abi_version", "qsft_status_string", "qsft_built_arch", "qsft_launch_count", "qsft_eval_cosets",
     "qsft_eval_cosets_tc", "qsft_eval_cosets_gemm", "qsft_gemm_layout", "qsft_eval_points",
-    "qsft_gwht", "qsft_add_noise_philox", "qsft_add_bins", "qsft_peel_init", "qsft_peel_iteration",
+    "qsft_gwht_noise", "qsft_gwht", "qsft_add_noise_philox", "qsft_add_bins", "qsft_peel_init", "qsft_peel_iteration",
     "qsft_peel_run", "qsft_collect", "qsft_rs_decode", "qsft_peel_noalloc", "qsft_workspace_layout",
 ]
 
@@ -115,6 +115,7 @@ def load():
         "qsft_gemm_layout": ([ctypes.POINTER(QsftJob), i32, plan_p, ctypes.POINTER(i64)], i32),
         "qsft_eval_points": ([i32, i32, i32, i32, vp, i64, vp, vp, vp, vp], i32),
         "qsft_gwht": ([i32, i32, i32, vp, vp, i64, vp], i32),
+        "qsft_gwht_noise": ([plan_p, i32, i32, vp, vp, i64, vp], i32),
         "qsft_add_noise_philox": ([plan_p, vp], i32),
         "qsft_add_bins": ([i32, vp, vp, i64, vp], i32),
         "qsft_peel_init": ([plan_p, vp], i32),

@@ -14,6 +14,7 @@
 #include <cooperative_groups.h>
 
 #include "common.cuh"
+#include "noise.cuh"
 
 namespace qsft {
 
@@ -174,10 +175,17 @@ __device__ __forceinline__ void groups_dft(V (&x)[16]) {
   }
 }
 
+// device bin noise of one row (noise.cuh); nu = 0: none
+struct RowNoise {
+  uint2 key;
+  int64_t row;  // row index within its job
+  double nu;
+};
+
 // one pass over digits [d0, d0 + m) with G = q^m; slo = stride of the lowest of them
 template <typename T, int Q, int G>
 __device__ __forceinline__ void row_pass(c2<T> (&x)[16], int t, int B, int slo, int mode, const c2<T>* src,
-                                         c2<T>* tile, c2<T>* dst, T scale) {
+                                         c2<T>* tile, c2<T>* dst, T scale, const RowNoise& nz) {
   const int nthr = B >> 4;
   int base[16 / G];
 #pragma unroll
@@ -194,42 +202,63 @@ __device__ __forceinline__ void row_pass(c2<T> (&x)[16], int t, int B, int slo, 
       x[k * G + m] = mode == 0 ? src[e] : tile[pad16(e)];
     }
   groups_dft<c2<T>, Q, G>(x);
-  // store: mode 2 to global (last pass, scaled), else to the tile
+  // store: mode 2 to global (last pass: scaled, plus the row's noise), else to
+  // the tile.  The last pass is over the top digits (its groups start below
+  // B/G), so entries m and m + G/2 of a group are e and e + B/2: one noise
+  // draw serves both.
+  if (mode == 2) {
+    const T tnu = (T)nz.nu;
 #pragma unroll
-  for (int k = 0; k < 16 / G; ++k)
+    for (int k = 0; k < 16 / G; ++k)
 #pragma unroll
-    for (int m = 0; m < G; ++m) {
-      const int e = base[k] + m * slo;
-      if (mode == 2) {
-        c2<T> v = x[k * G + m];
-        v.x *= scale;
-        v.y *= scale;
-        dst[e] = v;
-      } else {
-        tile[pad16(e)] = x[k * G + m];
+      for (int m = 0; m < G / 2; ++m) {
+        const int e0 = base[k] + m * slo, e1 = e0 + (G / 2) * slo;
+        c2<T> v0 = x[k * G + m], v1 = x[k * G + m + G / 2];
+        v0.x *= scale;
+        v0.y *= scale;
+        v1.x *= scale;
+        v1.y *= scale;
+        if (nz.nu > 0.0) {
+          c2<T> g0, g1;
+          noise_pair<T>(nz.key, nz.row, B / 2, e0, g0, g1);
+          v0.x += tnu * g0.x;
+          v0.y += tnu * g0.y;
+          v1.x += tnu * g1.x;
+          v1.y += tnu * g1.y;
+        }
+        dst[e0] = v0;
+        dst[e1] = v1;
       }
-    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 16 / G; ++k)
+#pragma unroll
+      for (int m = 0; m < G; ++m) tile[pad16(base[k] + m * slo)] = x[k * G + m];
+  }
 }
 
 template <typename T, int Q>
 __device__ __forceinline__ void row_pass_any(int nd, c2<T> (&v)[16], int t, int B, int slo, int mode, c2<T>* x,
-                                             c2<T>* tile, T scale) {
+                                             c2<T>* tile, T scale, const RowNoise& nz) {
   if constexpr (Q == 4) {
-    if (nd == 2) row_pass<T, 4, 16>(v, t, B, slo, mode, x, tile, x, scale);
-    else row_pass<T, 4, 4>(v, t, B, slo, mode, x, tile, x, scale);
+    if (nd == 2) row_pass<T, 4, 16>(v, t, B, slo, mode, x, tile, x, scale, nz);
+    else row_pass<T, 4, 4>(v, t, B, slo, mode, x, tile, x, scale, nz);
   } else {
-    if (nd == 4) row_pass<T, 2, 16>(v, t, B, slo, mode, x, tile, x, scale);
-    else if (nd == 3) row_pass<T, 2, 8>(v, t, B, slo, mode, x, tile, x, scale);
-    else if (nd == 2) row_pass<T, 2, 4>(v, t, B, slo, mode, x, tile, x, scale);
-    else row_pass<T, 2, 2>(v, t, B, slo, mode, x, tile, x, scale);
+    if (nd == 4) row_pass<T, 2, 16>(v, t, B, slo, mode, x, tile, x, scale, nz);
+    else if (nd == 3) row_pass<T, 2, 8>(v, t, B, slo, mode, x, tile, x, scale, nz);
+    else if (nd == 2) row_pass<T, 2, 4>(v, t, B, slo, mode, x, tile, x, scale, nz);
+    else row_pass<T, 2, 2>(v, t, B, slo, mode, x, tile, x, scale, nz);
   }
 }
 
 // rows of B = q^b >= 256 values: at least two passes (first from, last to global);
 // the top and the lowest DPP digits are disjoint full groups
+// jobs / row_meta (job, row within the job, per row) non-null: add each row's
+// device bin noise in the last pass
 template <typename T, int Q>
-__global__ void __launch_bounds__(sizeof(T) == 4 ? 1024 : 512) gwht_row_kernel(c2<T>* __restrict__ data, const int64_t* __restrict__ row_off,
-                                                        int64_t nrows, int b) {
+__global__ void __launch_bounds__(sizeof(T) == 4 ? 1024 : 512)
+    gwht_row_kernel(c2<T>* __restrict__ data, const int64_t* __restrict__ row_off, int64_t nrows, int b,
+                    const qsft_job* __restrict__ jobs, const int32_t* __restrict__ row_meta) {
   extern __shared__ __align__(16) unsigned char smem[];
   c2<T>* tile = reinterpret_cast<c2<T>*>(smem);
   constexpr int LQ = Q == 4 ? 2 : 1;  // bits per digit
@@ -246,30 +275,43 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 1024 : 512) gwht_row_kernel(c
       if (((reinterpret_cast<uintptr_t>(nx) | bytes) & 15) == 0)
         asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(nx), "r"(bytes) : "memory");
     }
+    RowNoise nz = {make_uint2(0, 0), 0, 0.0};
+    if (jobs) {
+      const qsft_job* jb = jobs + __ldg(row_meta + 2 * row);
+      nz.key = noise_key(jb->noise_seed);
+      nz.row = __ldg(row_meta + 2 * row + 1);
+      nz.nu = jb->noise_nu;
+    }
     c2<T> v[16];
-    // pass order (the digit axes are independent): the top DPP digits first
-    // (global reads, consecutive lanes on consecutive values), the lowest DPP
-    // next, then the groups in between from low to high -- the last pass,
-    // which writes global memory, is the one just below the top digits and
-    // its values are at least 16 apart, so lanes still cover whole lines
+    // pass order (the digit axes are independent): the groups between the
+    // top and the lowest DPP digits from high to low (the first reads global
+    // memory; its values are at least 16 apart, so lanes cover whole lines),
+    // then the lowest DPP digits, and the top DPP digits last: consecutive
+    // lanes store consecutive values, and each thread holds entries e and
+    // e + B/2 for the noise draws
+    const int nmid = npass - 2;
     for (int p = 0; p < npass; ++p) {
       int d0, d1;
-      if (p == 0) {
+      if (p < nmid) {
+        d1 = b - DPP - (nmid - 1 - p) * DPP;
+        d0 = d1 - DPP > DPP ? d1 - DPP : DPP;
+      } else if (p == nmid) {
+        d0 = b - DPP;
+        d1 = b;
+      } else {
         d0 = 0;
         d1 = DPP;
-      } else {
-        d1 = b - (p - 1) * DPP;
-        d0 = d1 - DPP > DPP ? d1 - DPP : DPP;
       }
       const int mode = p == 0 ? 0 : (p == npass - 1 ? 2 : 1);
-      row_pass_any<T, Q>(d1 - d0, v, t, B, 1 << (LQ * (b - d1)), mode, x, tile, scale);
+      row_pass_any<T, Q>(d1 - d0, v, t, B, 1 << (LQ * (b - d1)), mode, x, tile, scale, nz);
       __syncthreads();
     }
   }
 }
 
 template <typename T, int Q>
-static int launch_row(c2<T>* data, const int64_t* row_off, int64_t nrows, int b, cudaStream_t st) {
+static int launch_row(c2<T>* data, const int64_t* row_off, int64_t nrows, int b, cudaStream_t st,
+                      const qsft_job* jobs = nullptr, const int32_t* row_meta = nullptr) {
   const int LQ = Q == 4 ? 2 : 1;
   const int B = 1 << (LQ * b);
   const int threads = B / 16;
@@ -288,7 +330,7 @@ static int launch_row(c2<T>* data, const int64_t* row_off, int64_t nrows, int b,
   if (per < 1) per = 1;
   int64_t grid = (int64_t)sms * per;
   if (grid > nrows) grid = nrows;
-  kern<<<(unsigned)grid, threads, sm, st>>>(data, row_off, nrows, b);
+  kern<<<(unsigned)grid, threads, sm, st>>>(data, row_off, nrows, b, jobs, row_meta);
   QSFT_CUDA_CHECK_LAUNCH();
   return QSFT_OK;
 }
@@ -530,8 +572,37 @@ static int launch_pass(c2<T>* data, const int64_t* row_off, int64_t nrows, int q
   return QSFT_OK;
 }
 
+// device bin noise of listed rows (shapes the row kernel does not take)
 template <typename T>
-static int run_gwht(int q, int b, void* data, const int64_t* row_off, int64_t nrows, cudaStream_t st) {
+__global__ void noise_rows_kernel(c2<T>* __restrict__ data, const int64_t* __restrict__ row_off, int64_t nrows,
+                                  int64_t B, const qsft_job* __restrict__ jobs, const int32_t* __restrict__ row_meta) {
+  const int64_t half = (B + 1) / 2;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < nrows * half;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = p / half, e = p - i * half;
+    const qsft_job* jb = jobs + __ldg(row_meta + 2 * i);
+    const double nu = jb->noise_nu;
+    if (!(nu > 0.0)) continue;
+    c2<T> g0, g1;
+    noise_pair<T>(noise_key(jb->noise_seed), __ldg(row_meta + 2 * i + 1), half, e, g0, g1);
+    c2<T>* x = data + __ldg(row_off + i);
+    const T tnu = (T)nu;
+    c2<T> v = x[e];
+    v.x += tnu * g0.x;
+    v.y += tnu * g0.y;
+    x[e] = v;
+    if (e + half < B) {
+      c2<T> w = x[e + half];
+      w.x += tnu * g1.x;
+      w.y += tnu * g1.y;
+      x[e + half] = w;
+    }
+  }
+}
+
+template <typename T>
+static int run_gwht(int q, int b, void* data, const int64_t* row_off, int64_t nrows, cudaStream_t st,
+                    const qsft_job* jobs = nullptr, const int32_t* row_meta = nullptr) {
   const size_t es = sizeof(c2<T>);
   const size_t budget = 200 * 1024 - QSFT_MAX_Q * es;
   Pass passes[24];
@@ -543,7 +614,18 @@ static int run_gwht(int q, int b, void* data, const int64_t* row_off, int64_t nr
     const int bits = (q == 4 ? 2 : 1) * b;
     const int maxbits = sizeof(T) == 4 ? 14 : 13;  // whole row in shared memory
     if (bits >= 8 && bits <= maxbits)
-      return q == 4 ? launch_row<T, 4>(d, row_off, nrows, b, st) : launch_row<T, 2>(d, row_off, nrows, b, st);
+      return q == 4 ? launch_row<T, 4>(d, row_off, nrows, b, st, jobs, row_meta)
+                    : launch_row<T, 2>(d, row_off, nrows, b, st, jobs, row_meta);
+  }
+  if (jobs) {  // transform, then the listed rows' noise
+    const int rc = run_gwht<T>(q, b, data, row_off, nrows, st);
+    if (rc != QSFT_OK) return rc;
+    const int64_t B = ipow(q, b), pairs = nrows * ((B + 1) / 2);
+    const int64_t want = (pairs + 255) / 256;
+    noise_rows_kernel<T><<<(unsigned)(want < 152 * 8 ? want : 152 * 8), 256, 0, st>>>(d, row_off, nrows, B, jobs,
+                                                                                        row_meta);
+    QSFT_CUDA_CHECK_LAUNCH();
+    return QSFT_OK;
   }
   int k = 0;
   const int CS = cluster_split(q, b, es, &k);
@@ -574,6 +656,18 @@ static int run_gwht(int q, int b, void* data, const int64_t* row_off, int64_t nr
 }  // namespace qsft
 
 using namespace qsft;
+
+extern "C" int qsft_gwht_noise(const qsft_plan* plan, int q, int b, const int64_t* row_off, const int32_t* row_meta,
+                               int64_t nrows, qsft_stream_t stream) {
+  if (!plan || !plan->jobs || !plan->U || q < 2 || q > QSFT_MAX_Q || b < 1 || nrows < 0) return QSFT_ERR_ARG;
+  if (ipow(q, b) > (1LL << 22)) return QSFT_ERR_TOO_LARGE;
+  if (nrows == 0) return QSFT_OK;
+  if (!row_off || !row_meta) return QSFT_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  if (plan->prec == QSFT_F32) return run_gwht<float>(q, b, plan->U, row_off, nrows, st, plan->jobs, row_meta);
+  if (plan->prec == QSFT_F64) return run_gwht<double>(q, b, plan->U, row_off, nrows, st, plan->jobs, row_meta);
+  return QSFT_ERR_ARG;
+}
 
 extern "C" int qsft_gwht(int prec, int q, int b, void* data, const int64_t* row_off, int64_t nrows,
                          qsft_stream_t stream) {

@@ -1,70 +1,39 @@
 // Bin-domain complex AWGN (the noise of SyntheticSubsampledSignal.get_MDU,
-// synt_exp/synt_src/synthetic_signal.py:126-129), drawn on the device.
-//
-// Random bits: Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random
-// numbers: as easy as 1, 2, 3", SC 2011), counter = element index, key = the
-// job's noise_seed: a job draws the same noise whatever batch it is part of.  Normals: Box-Muller on the two pairs of words.
-#include "common.cuh"
+// synt_exp/synt_src/synthetic_signal.py:126-129), drawn on the device; the
+// stream is defined in noise.cuh.
+#include "noise.cuh"
 
 namespace qsft {
 
-__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
-  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
-#pragma unroll
-  for (int r = 0; r < 10; ++r) {
-    const uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
-    const uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
-    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
-    k.x += W0;
-    k.y += W1;
-  }
-  return c;
-}
-
-// two independent N(0,1) from two uniform words (Box-Muller), in T precision
-__device__ __forceinline__ double2 box_muller(uint32_t a, uint32_t b, double) {
-  const double u1 = ((double)a + 1.0) * 2.3283064365386963e-10;  // (0, 1]
-  const double u2 = (double)b * 2.3283064365386963e-10;          // [0, 1)
-  const double r = sqrt(-2.0 * log(u1));
-  double s, c;
-  sincospi(2.0 * u2, &s, &c);
-  return make_double2(r * c, r * s);
-}
-__device__ __forceinline__ float2 box_muller(uint32_t a, uint32_t b, float) {
-  const float u1 = ((float)(a >> 8) + 1.0f) * 5.9604645e-08f;  // (0, 1], 24-bit grid
-  const float u2 = (float)(b >> 8) * 5.9604645e-08f;           // [0, 1)
-  const float r = sqrtf(-2.0f * logf(u1));
-  float s, c;
-  sincospif(2.0f * u2, &s, &c);
-  return make_float2(r * c, r * s);
-}
-
+// thread per (row, e < half) pair of every job; rows [r0, r0 + nrows) of the
+// batch's row list when `rows` is given (row_off + row_meta), else all rows of
+// every job
 template <typename T>
 __global__ void noise_kernel(qsft_plan plan) {
   const int j = blockIdx.y;
   const qsft_job* job = plan.jobs + j;
   const double nu = job->noise_nu;
   if (!(nu > 0.0)) return;
-  const int64_t count = (int64_t)job->C * job->R * job->P * job->B;
+  const int64_t B = job->B, half = (B + 1) / 2;
+  const int64_t rows = (int64_t)job->C * job->R * job->P;
   c2<T>* U = reinterpret_cast<c2<T>*>(plan.U) + job->off_U;
-  const uint2 key = make_uint2((uint32_t)job->noise_seed, (uint32_t)(job->noise_seed >> 32));
-  // each thread draws 4 words -> 2 complex entries
-  for (int64_t pair = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; 2 * pair < count;
-       pair += (int64_t)gridDim.x * blockDim.x) {
-    const uint4 r = philox4x32_10(make_uint4((uint32_t)pair, (uint32_t)(pair >> 32), 0x9e37u, 0x51f7u), key);
-    const c2<T> g0 = box_muller(r.x, r.y, T(0));
-    const c2<T> g1 = box_muller(r.z, r.w, T(0));
-    const T tnu = (T)nu;
-    const int64_t e = 2 * pair;
-    c2<T> v = U[e];
+  const uint2 key = noise_key(job->noise_seed);
+  const T tnu = (T)nu;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < rows * half;
+       p += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t row = p / half, e = p - row * half;
+    c2<T> g0, g1;
+    noise_pair<T>(key, row, half, e, g0, g1);
+    c2<T>* x = U + row * B;
+    c2<T> v = x[e];
     v.x += tnu * g0.x;
     v.y += tnu * g0.y;
-    U[e] = v;
-    if (e + 1 < count) {
-      c2<T> w = U[e + 1];
+    x[e] = v;
+    if (e + half < B) {
+      c2<T> w = x[e + half];
       w.x += tnu * g1.x;
       w.y += tnu * g1.y;
-      U[e + 1] = w;
+      x[e + half] = w;
     }
   }
 }

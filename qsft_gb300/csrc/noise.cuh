@@ -1,0 +1,58 @@
+// Device bin noise shared by the noise kernels and the fused GWHT + noise pass.
+//
+// Random bits: Philox-4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random
+// numbers: as easy as 1, 2, 3", SC 2011) keyed by the job's noise_seed.  One
+// draw gives two complex normals (Box-Muller on each pair of words): for row
+// r (0 .. C*R*P - 1) of the job and e < half = ceil(q^b / 2), counter
+// r*half + e covers entries e and e + half of the row.  The noise of a job is
+// thus a function of its own seed and indices only, whatever batch it is in,
+// and a transform pass that holds entries e and e + half in one thread can add
+// it without another pass over the bins.
+#pragma once
+#include "common.cuh"
+
+namespace qsft {
+
+__device__ __forceinline__ uint4 philox4x32_10(uint4 c, uint2 k) {
+  const uint32_t M0 = 0xD2511F53u, M1 = 0xCD9E8D57u, W0 = 0x9E3779B9u, W1 = 0xBB67AE85u;
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+    const uint32_t hi0 = __umulhi(M0, c.x), lo0 = M0 * c.x;
+    const uint32_t hi1 = __umulhi(M1, c.z), lo1 = M1 * c.z;
+    c = make_uint4(hi1 ^ c.y ^ k.x, lo1, hi0 ^ c.w ^ k.y, lo0);
+    k.x += W0;
+    k.y += W1;
+  }
+  return c;
+}
+
+// two independent N(0,1) from two uniform words (Box-Muller), in T precision
+__device__ __forceinline__ double2 box_muller(uint32_t a, uint32_t b, double) {
+  const double u1 = ((double)a + 1.0) * 2.3283064365386963e-10;  // (0, 1]
+  const double u2 = (double)b * 2.3283064365386963e-10;          // [0, 1)
+  const double r = sqrt(-2.0 * log(u1));
+  double s, c;
+  sincospi(2.0 * u2, &s, &c);
+  return make_double2(r * c, r * s);
+}
+__device__ __forceinline__ float2 box_muller(uint32_t a, uint32_t b, float) {
+  const float u1 = ((float)(a >> 8) + 1.0f) * 5.9604645e-08f;  // (0, 1], 24-bit grid
+  const float u2 = (float)(b >> 8) * 5.9604645e-08f;           // [0, 1)
+  const float r = sqrtf(-2.0f * logf(u1));
+  float s, c;
+  sincospif(2.0f * u2, &s, &c);
+  return make_float2(r * c, r * s);
+}
+
+__device__ __forceinline__ uint2 noise_key(uint64_t seed) { return make_uint2((uint32_t)seed, (uint32_t)(seed >> 32)); }
+
+// the pair (entry e, entry e + half) of row `row`: standard normals, complex
+template <typename T>
+__device__ __forceinline__ void noise_pair(uint2 key, int64_t row, int64_t half, int64_t e, c2<T>& g0, c2<T>& g1) {
+  const uint64_t ctr = (uint64_t)row * (uint64_t)half + (uint64_t)e;
+  const uint4 r = philox4x32_10(make_uint4((uint32_t)ctr, (uint32_t)(ctr >> 32), 0x9e37u, 0x51f7u), key);
+  g0 = box_muller(r.x, r.y, T(0));
+  g1 = box_muller(r.z, r.w, T(0));
+}
+
+}  // namespace qsft

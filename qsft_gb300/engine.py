@@ -196,11 +196,14 @@ class Batch:
             self.tc_needs_zero |= chunks != 1
             tc_prefix.append(tc_prefix[-1] + chunks * groups)
         self.tc_prefix_host = tc_prefix
-        rows = {}
+        rows, meta = {}, {}
         for j, sp in enumerate(specs):
-            r = jobs[j].off_U + np.arange(sp.C * sp.R * sp.P, dtype=np.int64) * sp.B
-            rows.setdefault((sp.q, sp.b), []).append(r)
+            idx = np.arange(sp.C * sp.R * sp.P, dtype=np.int64)
+            rows.setdefault((sp.q, sp.b), []).append(jobs[j].off_U + idx * sp.B)
+            # (job, row within the job) per row: the key of the row's device noise
+            meta.setdefault((sp.q, sp.b), []).append(np.stack([np.full_like(idx, j), idx], axis=1).astype(np.int32))
         self.gwht_rows_host = {k: np.concatenate(v) for k, v in rows.items()}
+        self.gwht_meta_host = {k: np.concatenate(v).ravel() for k, v in meta.items()}
         self.max_iter = max(sp.max_iter for sp in specs)
 
     def _allocate(self):
@@ -217,6 +220,7 @@ class Batch:
         self.tc_prefix = up(np.array(self.tc_prefix_host, dtype=np.int64), torch.int64)
         self.gf = up(self.gf_host, torch.int32)
         self.gwht_groups = {k: up(v, torch.int64) for k, v in self.gwht_rows_host.items()}
+        self.gwht_meta = {k: up(v, torch.int32) for k, v in self.gwht_meta_host.items()}
         self.roots = roots_table(dev)
         self.rho = z(self.total_bins * 2, torch.float64)
         self.kbuf = z(self.total_bins * self.kstride, torch.uint8)
@@ -342,6 +346,13 @@ class Batch:
         else:
             raise ValueError(f"unknown evaluation method {method!r}")
 
+    def gwht_noise(self, stream=None):
+        """GWHT of every row, with each job's device bin noise added in the same pass."""
+        for (q, b), rows in self.gwht_groups.items():
+            check(self.lib.qsft_gwht_noise(ctypes.byref(self.plan), q, b, ctypes.c_void_p(rows.data_ptr()),
+                                           ctypes.c_void_p(self.gwht_meta[(q, b)].data_ptr()), rows.numel(),
+                                           stream_handle(stream)), "qsft_gwht_noise")
+
     def gwht(self, stream=None):
         for (q, b), rows in self.gwht_groups.items():
             check(self.lib.qsft_gwht(self.prec, q, b, ctypes.c_void_p(self.U.data_ptr()),
@@ -365,10 +376,9 @@ class Batch:
 
     # ------------------------------------------------------------ whole step
     def step(self, max_iter=None, stream=None):
-        """eval -> gwht -> noise -> peel -> collect, issued on the stream."""
+        """eval -> gwht + noise -> peel -> collect, issued on the stream."""
         self.eval(stream)
-        self.gwht(stream)
-        self.add_noise(stream)
+        self.gwht_noise(stream)
         self.peel(self.max_iter if max_iter is None else max_iter, stream)
         self.collect_async(stream)
 

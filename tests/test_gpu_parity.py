@@ -173,6 +173,29 @@ def test_device_noise_statistics(cuda):
     assert np.array_equal(bt2.job_U(0).cpu().numpy().ravel(), x), "same seed must give the same noise"
 
 
+@pytest.mark.parametrize("prec", PRECS)
+def test_fused_gwht_noise_equals_separate_passes(cuda, prec):
+    """qsft_gwht_noise (noise added in the transform's last pass, or after it for
+    shapes the row kernel does not take) == qsft_gwht then qsft_add_noise_philox."""
+    import torch
+    from qsft_gb300.engine import Batch, JobSpec
+    rng = np.random.RandomState(8)
+    specs = []
+    for (q, b, R, P, nu) in [(4, 6, 2, 9, 0.3), (2, 9, 1, 5, 0.2), (3, 5, 2, 4, 0.25), (4, 5, 1, 3, 0.0)]:
+        C = 2
+        U = torch.from_numpy(rng.randn(C, R * P, q ** b) + 1j * rng.randn(C, R * P, q ** b))
+        n = P - 1                                   # identity source: P - 1 >= n
+        specs.append(JobSpec(q, n, b, np.zeros((C, n, b)), np.zeros((C, R * P, n)), R, P, U=U, noise_nu=nu,
+                             noise_seed=77 + q))
+    a = Batch(specs, precision=prec)
+    a.gwht(); a.add_noise()
+    b_ = Batch(specs, precision=prec)
+    b_.gwht_noise()
+    for j in range(len(specs)):
+        x, y = a.job_U(j).cpu().numpy(), b_.job_U(j).cpu().numpy()
+        assert np.allclose(x, y, rtol=0, atol=1e-6 if prec == "fp32" else 1e-13), j
+
+
 def test_batch_of_mixed_shapes_equals_single_runs(cuda):
     """Jobs of different (q, n, b, C, R, P, S) in one packed batch give the
     same results as each alone."""
@@ -202,7 +225,7 @@ def test_batch_of_mixed_shapes_equals_single_runs(cuda):
         bt.eval(); bt.gwht(); bt.add_noise(); bt.peel()
         outs.append(bt.results()[0])
     bt = Batch(specs, precision="fp32")
-    bt.eval(); bt.gwht(); bt.add_noise(); bt.peel()
+    bt.eval(); bt.gwht_noise(); bt.peel()      # transform and noise fused in one pass
     mixed = bt.results()
     for (k1, v1, _, c1), (k2, v2, _, c2) in zip(outs, mixed):
         d1 = {tuple(k): v for k, v in zip(k1, v1)}
