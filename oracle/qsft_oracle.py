@@ -20,6 +20,7 @@ __all__ = [
     "random_signal_strength_model", "generate_signal_w", "get_Ms", "get_D", "get_Ms_and_Ds",
     "coset_points", "eval_points", "gwht", "subsample_qsft", "get_MDU_perm", "bin_noise",
     "singleton_detection", "peel", "OracleSignal", "OracleQSFT", "noise_sd_for_snr", "nmse", "closed_form_bins",
+    "test_qary_nmse",
 ]
 
 
@@ -396,3 +397,17 @@ def closed_form_bins(Ms, Ds, locq, strengths, q):
             np.add.at(U[r], jdec, vals[r])
         out.append(U)
     return np.array(out)
+
+
+def test_qary_nmse(beta, query_indices, samples, q, n):
+    """TestHelper._test_qary (qsft/test_helper.py:235-260): NMSE of the sparse
+    transform `beta` against `samples` at decimal `query_indices`; 1 when beta
+    is empty."""
+    if len(beta) == 0:
+        return 1
+    keys = np.array([list(k) for k in beta.keys()], dtype=np.int64).reshape(-1, n)
+    vals = np.array(list(beta.values()), dtype=np.complex128)
+    X = np.array([[(int(x) // q ** (n - 1 - i)) % q for i in range(n)] for x in query_indices], dtype=np.int64)
+    y_hat = np.exp(2j * np.pi * ((X @ keys.T) % q) / q) @ vals
+    samples = np.asarray(samples, dtype=np.complex128)
+    return float(np.linalg.norm(y_hat - samples) ** 2 / np.linalg.norm(samples) ** 2)

@@ -203,11 +203,43 @@ def gwht_pins():
     print("gwht_pins written")
 
 
+def test_qary_pins():
+    """TestHelper._test_qary (qsft/test_helper.py:235-260) on a recovered
+    transform with a few wrong and missing coefficients, at uniform test points
+    of the true signal: the reference method is called on a stand-in `self`
+    that carries only the attributes it reads (q, n, test_signal.signal_t)."""
+    from qsft.test_helper import TestHelper
+    rs = np.random.RandomState(321)
+    out = {}
+    for (q, n, S, N) in [(4, 10, 30, 2000), (3, 12, 20, 1500), (2, 20, 25, 3000)]:
+        locq = rs.randint(q, size=(S, n))
+        a = rs.uniform(1, 10, S) * np.exp(2j * np.pi * rs.uniform(size=S))
+        idx = rs.randint(0, q ** n, size=N)
+        X = np.array([[(int(x) // q ** (n - 1 - i)) % q for i in range(n)] for x in idx])
+        samples = np.exp(2j * np.pi * ((X @ locq.T) % q) / q) @ a
+        beta = {tuple(k): v * (1 + 0.01 * rs.randn()) for k, v in zip(map(tuple, locq[:-3]), a[:-3])}
+        stand_in = types.SimpleNamespace(q=q, n=n, test_signal=types.SimpleNamespace(
+            signal_t=dict(zip([int(x) for x in idx], samples))))
+        nmse = TestHelper._test_qary(stand_in, beta)
+        tag = f"q{q}_n{n}"
+        out[f"{tag}_keys"] = np.array(list(beta.keys()), dtype=np.int64)
+        out[f"{tag}_vals"] = np.array(list(beta.values()), dtype=np.complex128)
+        # the test points as the reference holds them: a dict, so repeated indices collapse
+        st = stand_in.test_signal.signal_t
+        out[f"{tag}_idx"] = np.array(list(st.keys()), dtype=np.int64)
+        out[f"{tag}_samples"] = np.array(list(st.values()), dtype=np.complex128)
+        out[f"{tag}_nmse"] = np.float64(nmse)
+    np.savez_compressed(os.path.join(HERE, "test_qary_pins.npz"), **out)
+    print("test_qary_pins written", {k: float(v) for k, v in out.items() if k.endswith("_nmse")})
+
+
 if __name__ == "__main__":
     _install_shims()
-    names = sys.argv[1:] or list(CASES) + ["gwht"]
+    names = sys.argv[1:] or list(CASES) + ["gwht", "test_qary"]
     for nm in names:
         if nm == "gwht":
             gwht_pins()
+        elif nm == "test_qary":
+            test_qary_pins()
         else:
             run_case(nm, CASES[nm])

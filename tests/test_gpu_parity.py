@@ -8,6 +8,8 @@ coefficients relative L2 <= 1e-5 against the reference's (noiseless and noisy
 alike, since the host draws the reference's noise), NMSE within 1% of the
 reference's NMSE.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -374,3 +376,47 @@ def test_generic_plugin_subsample(cuda):
                           reconstruct_method_channel="identity").transform(sig))
     assert set(res[0]) == set(res[1]) == set(syn.signal_w)
     assert max(abs(res[0][k] - res[1][k]) for k in res[0]) < 1e-4
+
+
+def test_test_nmse_matches_reference(cuda):
+    """The GPU time-domain test NMSE == the reference's _test_qary on the same inputs."""
+    from qsft_gb300.test_helper import test_nmse
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "test_qary_pins.npz"))
+    for tag in ("q4_n10", "q3_n12", "q2_n20"):
+        q, n = int(tag[1:tag.index("_")]), int(tag.split("_n")[1])
+        beta = {tuple(int(x) for x in k): v for k, v in zip(z[f"{tag}_keys"], z[f"{tag}_vals"])}
+        got = test_nmse(beta, z[f"{tag}_idx"], z[f"{tag}_samples"], q, n)
+        assert abs(got - float(z[f"{tag}_nmse"])) <= 1e-9 * float(z[f"{tag}_nmse"])
+    assert test_nmse({}, [0], [1.0], 4, 3) == 1
+
+
+def test_test_helper_end_to_end(cuda, tmp_path):
+    """TestHelper with a synthetic signal: train on coset samples (QSFT on the GPU),
+    test on uniform noiseless samples; the NMSE equals the oracle's on the same
+    recovered transform and is small at 20 dB."""
+    import qsft_gb300 as Q
+    from qsft_gb300.test_helper import TestHelper
+
+    class Synthetic(TestHelper):
+        def __init__(self, *a, **k):
+            np.random.seed(4)
+            sa = a[0]
+            _, self.locq, self.strengths = Q.generate_signal_w(sa["n"], sa["q"], sa["sparsity"], 1, 10, full=False)
+            super().__init__(*a, **k)
+
+        def generate_signal(self, signal_args):
+            args = dict(signal_args)
+            return Q.SyntheticSubsampledSignal(signal_w=None, locq=self.locq, strengths=self.strengths,
+                                               noise_sd=args.get("noise_sd", 0.0), n=args["n"], q=args["q"],
+                                               query_args=args["query_args"], folder=args["folder"])
+
+    S = 30
+    sa = dict(n=12, q=4, sparsity=S, noise_sd=O.noise_sd_for_snr(S, 20))
+    th = Synthetic(sa, ["qsft"], dict(num_subsample=3, num_repeat=2, b=5), dict(n_samples=3000), tmp_path)
+    np.random.seed(9)
+    beta = th.compute_model("qsft", dict(num_subsample=3, num_repeat=2, b=5, noise_sd=sa["noise_sd"]))
+    nmse = th.test_model("qsft", beta=beta)
+    ts = th.test_signal.signal_t
+    want = O.test_qary_nmse(beta, list(ts.keys()), list(ts.values()), 4, 12)
+    assert abs(nmse - want) <= 1e-9 * max(want, 1e-12)
+    assert nmse < 1e-2 and len(beta) >= S - 2

@@ -1,5 +1,7 @@
 """The oracle (a numpy restatement of the reference) against fixtures produced
 by running the reference itself (tests/golden/make_golden.py)."""
+import os
+
 import numpy as np
 import pytest
 
@@ -106,3 +108,15 @@ def test_oracle_all_bs_matches_reference():
     assert set(got) == set(want)
     assert max(abs(got[k] - want[k]) for k in want) < 1e-12
     assert res["n_samples"] == int(z["n_samples"])
+
+
+def test_oracle_test_qary_matches_reference():
+    """TestHelper._test_qary (qsft/test_helper.py:235-260) restated, against the
+    reference's own NMSE on the same recovered transform and test points."""
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "test_qary_pins.npz"))
+    for tag in ("q4_n10", "q3_n12", "q2_n20"):
+        q, n = int(tag[1:tag.index("_")]), int(tag.split("_n")[1])
+        beta = {tuple(int(x) for x in k): v for k, v in zip(z[f"{tag}_keys"], z[f"{tag}_vals"])}
+        got = O.test_qary_nmse(beta, z[f"{tag}_idx"], z[f"{tag}_samples"], q, n)
+        assert abs(got - float(z[f"{tag}_nmse"])) <= 1e-12 * float(z[f"{tag}_nmse"])
+    assert O.test_qary_nmse({}, [0], [1.0], 4, 3) == 1
