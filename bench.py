@@ -169,7 +169,7 @@ def run_ours(args):
     import torch.distributed as dist
     from qsft_gb300 import _lib
     from qsft_gb300.engine import Batch
-    from qsft_gb300.serve import transform_batch
+    from qsft_gb300.serve import TransformStream, transform_batch
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -250,21 +250,41 @@ def run_ours(args):
     found = [len(set(map(tuple, k.tolist())) & t) for (k, _, _, _), t in zip(res, truth)]
     iters = [int(c.iter) for (_, _, _, c) in res]
 
-    # ---- end to end through the public API, host buffers
+    # ---- end to end through the public API, host buffers: a TransformStream
+    # pipelines the steps (host packing / parsing of one batch overlaps the
+    # GPU's work on the next); every step still packs and uploads its inputs
+    # and reads back its results inside the timed region
+    ts = TransformStream(precision=args.precision)
+    for _ in range(max(args.warmup, 3)):
+        t_a = ts.submit(reqs)
+        t_b = ts.submit(reqs)
+        ts.result(t_a)
+        ts.result(t_b)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    prev = None
+    for i in range(args.steps):
+        tk = ts.submit(reqs)
+        if prev is not None:
+            ts.result(prev)
+        prev = tk
+    ts.result(prev)
+    torch.cuda.synchronize()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e = J * args.steps * world / e2e_s
+    b2 = ts.last_batch()
+    h2d = int(b2.h2d_bytes)
+    d2h = int(b2.d2h_bytes)
+    # batch completion latency: one synchronous call at a time
     lat = []
-    h2d = d2h = 0
     for i in range(max(args.warmup, 3) + args.steps):
         barrier()
         t = time.perf_counter()
-        out, b2 = transform_batch(reqs, precision=args.precision, return_batch=True)
+        transform_batch(reqs, precision=args.precision)
         torch.cuda.synchronize()
-        dt = time.perf_counter() - t
         if i >= max(args.warmup, 3):
-            lat.append(dt)
-    h2d = int(b2.h2d_bytes)
-    d2h = int(b2.d2h_bytes)
-    e2e_s = max_over_ranks(float(np.sum(lat)))
-    e2e = J * len(lat) * world / e2e_s
+            lat.append(time.perf_counter() - t)
 
     # ---- FP64 plain: one transform per launch sequence, FP64 everywhere
     b64 = Batch([reqs[0].spec()], precision="fp64", device=dev)

@@ -407,13 +407,49 @@ class Batch:
         extra = max(max(int(c.iter) for c in ctrl) - 2, -1)
         return self.graph_launches + _lib.PEEL_LAUNCHES_PER_ITER * extra
 
-    def run(self):
-        """One step: graph replay when captured, else direct launches."""
-        g = getattr(self, "graph", None)
-        if g is not None:
-            g.replay()
-        else:
-            self.step()
+    def run(self, stream=None):
+        """One step on `stream` (default: the current stream): graph replay when
+        captured, else direct launches."""
+        st = stream if stream is not None else torch.cuda.current_stream(self.device)
+        with torch.cuda.stream(st):
+            g = getattr(self, "graph", None)
+            if g is not None:
+                g.replay()
+            else:
+                self.step()
+
+    def fetch_async(self, stream=None, rows_hint=None):
+        """Queue the result read-back on `stream` without waiting: the metadata and
+        the first `rows_hint` output rows go to pinned host buffers, and an event
+        marks their arrival (``results_fetched`` waits on it)."""
+        st = stream if stream is not None else torch.cuda.current_stream(self.device)
+        if not hasattr(self, "out_k_host"):
+            self.out_k_host = torch.empty_like(self.out_k, device="cpu").pin_memory()
+            self.out_val_host = torch.empty_like(self.out_val, device="cpu").pin_memory()
+            self.out_cnt_host = torch.empty_like(self.out_cnt, device="cpu").pin_memory()
+            self.fetched_event = torch.cuda.Event()
+        rows = self.total_balls if rows_hint is None else int(min(max(rows_hint, 1), self.total_balls))
+        with torch.cuda.stream(st):
+            self.meta_host.copy_(self.meta, non_blocking=True)
+            self.out_k_host[:rows * self.kstride].copy_(self.out_k[:rows * self.kstride], non_blocking=True)
+            self.out_val_host[:rows * 2].copy_(self.out_val[:rows * 2], non_blocking=True)
+            self.out_cnt_host[:rows].copy_(self.out_cnt[:rows], non_blocking=True)
+            self.fetched_event.record(st)
+        self.fetched_rows = rows
+
+    def results_fetched(self):
+        """``results()`` from the buffers ``fetch_async`` filled: waits for its event;
+        rows beyond the prefix it copied (rare: more recovered keys than the hint)
+        are read now."""
+        self.fetched_event.synchronize()
+        meta = self.meta_host.numpy()
+        total = int(meta[0])
+        if total > self.fetched_rows:
+            a, z = self.fetched_rows, total
+            self.out_k_host[a * self.kstride:z * self.kstride].copy_(self.out_k[a * self.kstride:z * self.kstride])
+            self.out_val_host[a * 2:z * 2].copy_(self.out_val[a * 2:z * 2])
+            self.out_cnt_host[a:z].copy_(self.out_cnt[a:z])
+        return self._parse(meta, self.out_k_host.numpy(), self.out_val_host.numpy(), self.out_cnt_host.numpy())
 
     def collect_async(self, stream=None):
         check(self.lib.qsft_collect(ctypes.byref(self.plan), ctypes.c_void_p(self.out_k.data_ptr()),
@@ -440,6 +476,11 @@ class Batch:
         if not collected:
             self.collect_async(stream)
         meta = self._read_meta()
+        rows = max(int(meta[0]), 1)
+        return self._parse(meta, self.out_k[:rows * self.kstride].cpu().numpy(),
+                           self.out_val[:rows * 2].cpu().numpy(), self.out_cnt[:rows].cpu().numpy())
+
+    def _parse(self, meta, out_k, out_val, out_cnt):
         J = self.njobs
         total = int(meta[0])
         idx = meta[1:1 + 2 * J].reshape(-1, 2)
@@ -449,9 +490,9 @@ class Batch:
             st = st - (1 << 32) if st >= (1 << 31) else st
             raise _lib.QsftError(f"device status {st}: {self.lib.qsft_status_string(st).decode()}")
         rows = max(total, 1)
-        ks = self.out_k[:rows * self.kstride].cpu().numpy().reshape(-1, self.kstride)
-        vals = self.out_val[:rows * 2].cpu().numpy().reshape(-1, 2)
-        cnts = self.out_cnt[:rows].cpu().numpy()
+        ks = out_k[:rows * self.kstride].reshape(-1, self.kstride)
+        vals = out_val[:rows * 2].reshape(-1, 2)
+        cnts = out_cnt[:rows]
         self.d2h_bytes = self.meta.numel() * 8 + rows * (self.kstride + 16 + 4)
         out = []
         for j, shape in enumerate(self.shapes):

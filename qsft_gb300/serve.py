@@ -5,8 +5,10 @@ host (support, coefficients, query matrices, noise level); ``transform_batch``
 packs any number of requests -- of any mix of shapes -- into one
 :class:`~qsft_gb300.engine.Batch`, runs evaluation, GWHT, device noise and
 peeling as one launch per phase, and returns one ``TransformResult`` (arrays;
-``to_dict()`` gives the reference's ``{k: coefficient}``) per request.  This is
-the call the serving loop and the benchmark make.
+``to_dict()`` gives the reference's ``{k: coefficient}``) per request.
+``TransformStream`` pipelines successive batches (host packing and result
+parsing overlap the GPU's work on the previous batch); it is what the
+end-to-end benchmark drives.
 """
 from collections import OrderedDict
 
@@ -123,3 +125,78 @@ def transform_batch(requests, precision="fp32", return_batch=False):
     out = [TransformResult(keys, vals, cnts, int(ctrl.iter))
            for keys, vals, cnts, ctrl in batch.results(collected=True)]
     return (out, batch) if return_batch else out
+
+
+def _rows_hint(requests):
+    """Output rows to read back without waiting: about twice the supports."""
+    return sum(2 * r.S + 64 for r in requests)
+
+
+class TransformStream:
+    """Pipelined batches: ``submit`` packs and uploads a batch and queues its
+    step and result read-back on a CUDA stream of its own, returning at once;
+    ``result`` waits for that batch and returns its TransformResults.
+
+    Each layout gets a ring of `depth` workspaces (each with its captured step
+    and its own stream), so the host packs batch k+1 -- and parses batch k-1 --
+    while the GPU runs batch k.  A workspace is reused only after its previous
+    batch's results have been collected (``submit`` collects them itself if the
+    caller has not), so its pinned staging buffers are never overwritten while
+    a copy from them is pending."""
+
+    def __init__(self, precision="fp32", depth=2, device=None):
+        self.precision, self.depth = precision, int(depth)
+        self.device = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+        self._rings = {}       # layout key -> list of [batch, stream, ticket in flight or None]
+        self._cursor = {}
+        self._inflight = {}    # ticket -> (slot, number of requests)
+        self._done = {}        # tickets collected early (their slot was needed)
+        self._next = 0
+
+    def submit(self, requests):
+        requests = list(requests)
+        specs = [r.spec() for r in requests]
+        max_iter = max(r.max_iter for r in requests)
+        key = (max_iter, tuple(layout_key(s) for s in specs))
+        ring = self._rings.setdefault(key, [])
+        cur = self._cursor.get(key, 0)
+        if len(ring) < self.depth:
+            b = Batch(specs, precision=self.precision, device=self.device)
+            b.capture(max_iter)
+            ring.append([b, torch.cuda.Stream(self.device), None])
+            cur = len(ring) - 1
+        slot = ring[cur]
+        self._cursor[key] = (cur + 1) % self.depth
+        if slot[2] is not None:            # the slot's previous batch: collect it first
+            prev = slot[2]
+            self._done[prev] = self._collect(prev)
+        batch, st = slot[0], slot[1]
+        st.wait_stream(torch.cuda.current_stream(self.device))
+        batch.load(specs, stream=st)
+        batch.run(st)
+        batch.fetch_async(st, _rows_hint(requests))
+        ticket = self._next
+        self._next += 1
+        slot[2] = ticket
+        self._inflight[ticket] = (slot, len(requests))
+        return ticket
+
+    def _collect(self, ticket):
+        slot, _ = self._inflight.pop(ticket)
+        slot[2] = None
+        return [TransformResult(keys, vals, cnts, int(ctrl.iter))
+                for keys, vals, cnts, ctrl in slot[0].results_fetched()]
+
+    def result(self, ticket):
+        """The TransformResults of a submitted batch (waits for it)."""
+        if ticket in self._done:
+            return self._done.pop(ticket)
+        if ticket not in self._inflight:
+            raise KeyError(f"unknown or already collected ticket {ticket}")
+        return self._collect(ticket)
+
+    def last_batch(self, ticket=None):
+        """The workspace that ran the most recent (or the given in-flight) batch."""
+        if ticket is not None and ticket in self._inflight:
+            return self._inflight[ticket][0][0]
+        return max((s for r in self._rings.values() for s in r), key=lambda s: -1 if s[2] is None else s[2])[0]

@@ -420,3 +420,25 @@ def test_test_helper_end_to_end(cuda, tmp_path):
     want = O.test_qary_nmse(beta, list(ts.keys()), list(ts.values()), 4, 12)
     assert abs(nmse - want) <= 1e-9 * max(want, 1e-12)
     assert nmse < 1e-2 and len(beta) >= S - 2
+
+
+def test_transform_stream_matches_transform_batch(cuda):
+    """Pipelined TransformStream (ring of captured workspaces per layout, async
+    read-back) returns what transform_batch returns, for interleaved layouts and
+    more submissions in flight than the ring holds."""
+    from qsft_gb300.serve import TransformStream, random_request, transform_batch
+    np.random.seed(31)
+    groups = [[random_request(4, 12, 5, 60, C=3, R=2, snr_db=20.0) for _ in range(3)] for _ in range(3)]
+    groups += [[random_request(2, 14, 8, 40, C=3, R=2, snr_db=20.0) for _ in range(2)] for _ in range(2)]
+    ts = TransformStream(depth=2)
+    tickets = [ts.submit(g) for g in groups]          # 5 submissions, rings of 2: early collection
+    got = [ts.result(t) for t in reversed(tickets)][::-1]
+    for g, res in zip(groups, got):
+        want = transform_batch(g)
+        for a, b in zip(res, want):
+            da, db = a.to_dict(), b.to_dict()
+            assert set(da) == set(db) and len(da) > 0
+            assert max(abs(da[k] - db[k]) for k in da) < 1e-6
+            assert a.iterations == b.iterations
+    with pytest.raises(KeyError):
+        ts.result(tickets[0])
