@@ -8,7 +8,7 @@
 //                 previous subtractions changed (the rest keep their class:
 //                 it is a function of the bin's unchanged values), and the
 //                 multiton count is kept up to date as classes change.
-//   decode        warp per queued bin: channel decoding of k (noiseless
+//   decode        a group of 8 threads per queued bin: channel decoding of k (noiseless
 //                 qsft/reconstruct.py:12-31 or NSO "nso1" :100-113, lanes over
 //                 symbols), optional Reed-Solomon source decoding (:34-51),
 //                 projection rho = <omega^(Dk), col>/len and residual energy
@@ -39,6 +39,7 @@ constexpr int SCAN_THREADS = 256;
 constexpr int WARPS_PER_BLOCK = 8;
 constexpr int MAX_SYMS = 256;  // channel symbols per bin (P - 1 <= 256)
 constexpr int LIST_BLOCKS = 152 * 8;
+constexpr int DEC_BLOCKS = 152 * 12;
 
 // ---------------------------------------------------------------- helpers
 __device__ __forceinline__ uint32_t hash_row(const uint8_t* row, int words) {
@@ -201,201 +202,239 @@ __device__ __forceinline__ bool krow_eq(const uint8_t* mine, const uint8_t* othe
   return eq;
 }
 
+// A group of DEC_G threads per queued bin (DEC_G consecutive lanes; a warp
+// holds 32 / DEC_G bins): symbols, rows and digits are dealt over the group
+// and its sums reduced with in-group shuffles, so every bin of an iteration
+// is in flight at once (first iteration: ~50K bins) while the dependent chain
+// of one bin stays short (later iterations: a few thousand).  A warp works on
+// bins of one job (chunks dealt round-robin), so control flow is uniform.
+// The column's RP values (stride B in U) are staged in shared memory with one
+// round of loads when RP <= DEC_STAGE_RP; FP32 roots for every q come from a
+// block-wide table.
+constexpr int DEC_THREADS = 128;
+constexpr int DEC_G = 8;
+constexpr int DEC_CPW = 32 / DEC_G;                    // bins per warp at a time
+constexpr int DEC_BINS = DEC_THREADS / DEC_G;          // bins per block at a time
+constexpr int DEC_STAGE_RP = 64;
+constexpr int DEC_KB = QSFT_MAX_N + 16;
+
+template <typename V>
+__device__ __forceinline__ V group_sum(V v, unsigned mask) {
+#pragma unroll
+  for (int o = DEC_G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+  return v;
+}
+
 template <typename T>
-__global__ void __launch_bounds__(WARPS_PER_BLOCK * 32, 3) decode_kernel(qsft_plan plan) {
+__global__ void __launch_bounds__(DEC_THREADS, 4) decode_kernel(qsft_plan plan) {
   if (__ldcg(plan.done_count) >= plan.njobs) return;  // every job has left the loop
-  __shared__ __align__(16) uint8_t s_k[WARPS_PER_BLOCK][QSFT_MAX_N + 16];
-  __shared__ uint8_t s_sym[WARPS_PER_BLOCK][MAX_SYMS];
-  __shared__ c2<T> s_col[WARPS_PER_BLOCK][STAGE_RP];
-  __shared__ float2 s_w[WARPS_PER_BLOCK][QSFT_MAX_Q];  // exp(2 pi i m / q) of the current job, FP32
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const int gw = blockIdx.x * WARPS_PER_BLOCK + wib;
-  const int nw = gridDim.x * WARPS_PER_BLOCK;
-  uint8_t* kl = s_k[wib];
-  uint8_t* syms = s_sym[wib];
-  c2<T>* sc = s_col[wib];
-  int64_t base = 0;  // items of all jobs are dealt round-robin to the warps of the grid
+  __shared__ float2 s_w[33 * 32];                            // roots, FP32
+  __shared__ c2<T> s_col[DEC_BINS][DEC_STAGE_RP];
+  __shared__ __align__(16) uint8_t s_k[DEC_BINS][DEC_KB];
+  __shared__ uint8_t s_sym[DEC_BINS][MAX_SYMS];
+  for (int i = threadIdx.x; i < 33 * 32; i += blockDim.x)
+    s_w[i] = make_float2((float)plan.roots[2 * i], (float)plan.roots[2 * i + 1]);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, gi = lane % DEC_G;
+  const int slot = threadIdx.x / DEC_G;                      // the block's bin slot of this group
+  const unsigned gmask = ((1u << DEC_G) - 1) << (lane - gi);
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  const int ks = plan.kstride;
+  c2<T>* sc = s_col[slot];
+  uint8_t* kl = s_k[slot];
+  int64_t chunk0 = 0;
   for (int jid = 0; jid < plan.njobs; ++jid) {
     qsft_ctrl* ctl = plan.ctrl + jid;
     if (ctl->done) continue;
     const int cnt = ctl->n_cand;
-    const int start = (int)(((int64_t)gw - base) % nw + nw) % nw;
-    base += cnt;
-    if (start >= cnt) continue;
+    const int nch = (cnt + DEC_CPW - 1) / DEC_CPW;
+    const int start = (int)(((int64_t)gw - chunk0) % nw + nw) % nw;
+    chunk0 += nch;
+    if (start >= nch) continue;
     const qsft_job* __restrict__ job = plan.jobs + jid;
     const int q = job->q, n = job->n, b = job->b, B = job->B, P = job->P, R = job->R;
     const int RP = R * P, nsym = P - 1;
     const double thr = job->cutoff * RP;
-    const int ks = plan.kstride;
-    const bool staged = RP <= STAGE_RP;
+    const bool staged = RP <= DEC_STAGE_RP;
     const bool words_ok = (n & 3) == 0 && ((job->off_D & 3) == 0);
-    if (lane < q) s_w[wib][lane] = make_float2((float)plan.roots[(q * 32 + lane) * 2], (float)plan.roots[(q * 32 + lane) * 2 + 1]);
-    __syncwarp();
-    for (int u = start; u < cnt; u += nw) {
-      const int local = plan.cand[job->off_bin + u];
+    const float2* wq = s_w + q * 32;
+    uint8_t* syms = job->src == QSFT_SRC_CODED ? s_sym[slot] : kl;
+    for (int ch = start; ch < nch; ch += nw) {   // uniform over the warp: every lane runs every sync
+      const int u = ch * DEC_CPW + lane / DEC_G;
+      const bool active = u < cnt;
+      const int local = active ? plan.cand[job->off_bin + u] : 0;
       const int c = local / B, jb = local - (local / B) * B;
       const int64_t gb = job->off_bin + local;
       const c2<T>* col = reinterpret_cast<const c2<T>*>(plan.U) + job->off_U + (int64_t)c * RP * B + jb;
-      // the column's RP values (stride B) in one round of loads
-      if (staged) {
-        for (int r = lane; r < RP; r += 32) sc[r] = col[(int64_t)r * B];
-        __syncwarp();
-      }
+      if (staged && active)
+        for (int r = gi; r < RP; r += DEC_G) sc[r] = col[(int64_t)r * B];
+      __syncwarp();
       auto V = [&](int r) -> c2<T> { return staged ? sc[r] : col[(int64_t)r * B]; };
-      // ---- channel decoding, lanes over symbols
-      if (job->chan == QSFT_CHAN_IDENTITY) {
-        const c2<T> v0 = V(0);
-        const T a0 = atan2(v0.y, v0.x);
-        for (int i = lane + 1; i < RP && i <= nsym; i += 32) {
-          const c2<T> vi = V(i);
-          const T ai = atan2(vi.y, vi.x);
-          double a = (double)((T)q * (ai - a0) / (T)6.283185307179586);
-          if (sizeof(T) == 4 && fabs(a - floor(a) - 0.5) < 1e-3)
-            a = (double)q * (atan2((double)vi.y, (double)vi.x) - atan2((double)v0.y, (double)v0.x)) /
-                6.283185307179586;
-          long long m = (long long)rint(a);  // round half to even, like np.round
-          m %= q;
-          if (m < 0) m += q;
-          syms[i - 1] = (uint8_t)m;
-        }
-      } else {
-        for (int i = lane + 1; i <= nsym; i += 32) {
-          T zr = 0, zi = 0;
-          for (int r = 0; r < R; ++r) {
-            const c2<T> u0 = V(r * P), ui = V(r * P + i);
-            zr += u0.x * ui.x + u0.y * ui.y;
-            zi += u0.y * ui.x - u0.x * ui.y;
+      // ---- channel decoding, symbols dealt over the group
+      if (active) {
+        if (job->chan == QSFT_CHAN_IDENTITY) {
+          const c2<T> v0 = V(0);
+          const T a0 = atan2(v0.y, v0.x);
+          for (int i = 1 + gi; i < RP && i <= nsym; i += DEC_G) {
+            const c2<T> vi = V(i);
+            const T ai = atan2(vi.y, vi.x);
+            double a = (double)((T)q * (ai - a0) / (T)6.283185307179586);
+            if (sizeof(T) == 4 && fabs(a - floor(a) - 0.5) < 1e-3)
+              a = (double)q * (atan2((double)vi.y, (double)vi.x) - atan2((double)v0.y, (double)v0.x)) /
+                  6.283185307179586;
+            long long m = (long long)rint(a);  // round half to even, like np.round
+            m %= q;
+            if (m < 0) m += q;
+            syms[i - 1] = (uint8_t)m;
           }
-          if (sizeof(T) == 4) {
-            float ang = atan2f((float)zi, (float)zr);
-            if (ang < 0.f) ang += 6.28318530717958647f;
-            const float tq = ang * (float)q * 0.15915494309189535f;
-            if (fabsf(tq - floorf(tq) - 0.5f) >= 1e-3f) {
-              // away from a tie the nearest of 2 pi m / q, m = 0..q, is floor(tq + 1/2)
-              syms[i - 1] = (uint8_t)(((int)floorf(tq + 0.5f)) % q);
-              continue;
-            }
-            double dzr = 0, dzi = 0;  // near a rounding boundary: recompute in FP64
+        } else {
+          for (int i = 1 + gi; i <= nsym; i += DEC_G) {
+            T zr = 0, zi = 0;
             for (int r = 0; r < R; ++r) {
-              const double2 u0 = to_d2(V(r * P)), ui = to_d2(V(r * P + i));
-              dzr += u0.x * ui.x + u0.y * ui.y;
-              dzi += u0.y * ui.x - u0.x * ui.y;
+              const c2<T> u0 = V(r * P), ui = V(r * P + i);
+              zr += u0.x * ui.x + u0.y * ui.y;
+              zi += u0.y * ui.x - u0.x * ui.y;
             }
-            double ang64 = atan2(dzi, dzr);
-            if (ang64 < 0) ang64 += 6.283185307179586;
-            syms[i - 1] = (uint8_t)nearest_root(ang64, q);
-          } else {
-            double ang = (double)atan2(zi, zr);
-            if (ang < 0) ang += 6.283185307179586;
-            syms[i - 1] = (uint8_t)nearest_root(ang, q);
+            if (sizeof(T) == 4) {
+              float ang = atan2f((float)zi, (float)zr);
+              if (ang < 0.f) ang += 6.28318530717958647f;
+              const float tq = ang * (float)q * 0.15915494309189535f;
+              if (fabsf(tq - floorf(tq) - 0.5f) >= 1e-3f) {
+                // away from a tie the nearest of 2 pi m / q, m = 0..q, is floor(tq + 1/2)
+                syms[i - 1] = (uint8_t)(((int)floorf(tq + 0.5f)) % q);
+                continue;
+              }
+              double dzr = 0, dzi = 0;  // near a rounding boundary: recompute in FP64
+              for (int r = 0; r < R; ++r) {
+                const double2 u0 = to_d2(V(r * P)), ui = to_d2(V(r * P + i));
+                dzr += u0.x * ui.x + u0.y * ui.y;
+                dzi += u0.y * ui.x - u0.x * ui.y;
+              }
+              double ang64 = atan2(dzi, dzr);
+              if (ang64 < 0) ang64 += 6.283185307179586;
+              syms[i - 1] = (uint8_t)nearest_root(ang64, q);
+            } else {
+              double ang = (double)atan2(zi, zr);
+              if (ang < 0) ang += 6.283185307179586;
+              syms[i - 1] = (uint8_t)nearest_root(ang, q);
+            }
           }
         }
       }
       __syncwarp();
       // ---- source decoding
-      if (job->src == QSFT_SRC_CODED) {
-        if (lane == 0) {
-          const GFt g = make_gf(plan.gf_tables + job->rs_gf_off, q, job->rs_s);
-          rs_decode(g, q, job->rs_s, job->rs_t, n, syms, kl);
-        }
-      } else {
-        for (int i = lane; i < n; i += 32) kl[i] = syms[i];
+      if (job->src == QSFT_SRC_CODED && active && gi == 0) {
+        const GFt g = make_gf(plan.gf_tables + job->rs_gf_off, q, job->rs_s);
+        rs_decode(g, q, job->rs_s, job->rs_t, n, syms, kl);
       }
       __syncwarp();
-      for (int i = n + lane; i < ks; i += 32) kl[i] = 0;
+      for (int i = n + gi; i < ks; i += DEC_G) kl[i] = 0;
       __syncwarp();
-      // ---- projection rho = <omega^(Dk), col> / RP and residual energy, lanes
-      //      over rows (phases of the first 4*32 rows kept in registers).
-      //      FP64 plans compute both in FP64; FP32 plans in FP32 (their bins
-      //      are FP32), recomputing in FP64 when the residual falls within 1%
-      //      of the singleton threshold.
+      // ---- projection rho = <omega^(Dk), col> / RP and residual energy, rows
+      //      dealt over the group: FP32 for FP32 plans (FP64 within 1% of the
+      //      threshold), FP64 for FP64 plans
       const int8_t* Dc = plan.i8 + job->off_D + (int64_t)c * RP * n;
-      int phc[4];
-#pragma unroll
-      for (int k = 0; k < 4; ++k) {
-        const int r = lane + 32 * k;
-        phc[k] = r < RP ? row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q) : 0;
-      }
-      auto each_row = [&](auto&& f) {  // f(phase, row) over this lane's rows
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-          if (lane + 32 * k < RP) f(phc[k], lane + 32 * k);
-        for (int r = lane + 128; r < RP; r += 32) f(row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q), r);
-      };
       auto project64 = [&](double2& rho_out, double& res_out) {
         double ar = 0, ai = 0;
-        each_row([&](int ph, int r) {
-          const double2 w = root(plan.roots, q, ph);
+        for (int r = gi; r < RP; r += DEC_G) {
+          const double2 w = root(plan.roots, q, row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q));
           const double2 v = to_d2(V(r));
           ar += w.x * v.x + w.y * v.y;
           ai += w.x * v.y - w.y * v.x;
-        });
-        ar = warp_sum(ar);
-        ai = warp_sum(ai);
+        }
+        ar = group_sum(ar, gmask);
+        ai = group_sum(ai, gmask);
         const double2 rh = make_double2(ar / RP, ai / RP);
         double rs = 0;
-        each_row([&](int ph, int r) {
-          const double2 w = root(plan.roots, q, ph);
+        for (int r = gi; r < RP; r += DEC_G) {
+          const double2 w = root(plan.roots, q, row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q));
           const double2 v = to_d2(V(r));
           const double dx = v.x - (rh.x * w.x - rh.y * w.y);
           const double dy = v.y - (rh.x * w.y + rh.y * w.x);
           rs += dx * dx + dy * dy;
-        });
+        }
         rho_out = rh;
-        res_out = warp_sum(rs);
+        res_out = group_sum(rs, gmask);
       };
-      double2 rho;
-      double res;
+      double2 rho = make_double2(0.0, 0.0);
+      double res = 0.0;
       if (sizeof(T) == 4) {
-        const float2* wt = s_w[wib];
+        int ph[(DEC_STAGE_RP + DEC_G - 1) / DEC_G];
         float ar = 0.f, ai = 0.f;
-        each_row([&](int ph, int r) {
-          const float2 w = wt[ph];
+#pragma unroll
+        for (int k = 0; k < (DEC_STAGE_RP + DEC_G - 1) / DEC_G; ++k) {
+          const int r = gi + k * DEC_G;
+          ph[k] = 0;
+          if (r < RP) {
+            ph[k] = row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q);
+            const float2 w = wq[ph[k]];
+            const c2<T> v = V(r);
+            ar += w.x * (float)v.x + w.y * (float)v.y;
+            ai += w.x * (float)v.y - w.y * (float)v.x;
+          }
+        }
+        for (int r = gi + DEC_STAGE_RP; r < RP; r += DEC_G) {  // rows past the register-held phases
+          const float2 w = wq[row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q)];
           const c2<T> v = V(r);
           ar += w.x * (float)v.x + w.y * (float)v.y;
           ai += w.x * (float)v.y - w.y * (float)v.x;
-        });
-        ar = warp_sum_f(ar) / (float)RP;
-        ai = warp_sum_f(ai) / (float)RP;
+        }
+        ar = group_sum(ar, gmask) / (float)RP;
+        ai = group_sum(ai, gmask) / (float)RP;
         float rs = 0.f;
-        each_row([&](int ph, int r) {
-          const float2 w = wt[ph];
+#pragma unroll
+        for (int k = 0; k < (DEC_STAGE_RP + DEC_G - 1) / DEC_G; ++k) {
+          const int r = gi + k * DEC_G;
+          if (r < RP) {
+            const float2 w = wq[ph[k]];
+            const c2<T> v = V(r);
+            const float dx = (float)v.x - (ar * w.x - ai * w.y);
+            const float dy = (float)v.y - (ar * w.y + ai * w.x);
+            rs += dx * dx + dy * dy;
+          }
+        }
+        for (int r = gi + DEC_STAGE_RP; r < RP; r += DEC_G) {
+          const float2 w = wq[row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q)];
           const c2<T> v = V(r);
           const float dx = (float)v.x - (ar * w.x - ai * w.y);
           const float dy = (float)v.y - (ar * w.y + ai * w.x);
           rs += dx * dx + dy * dy;
-        });
+        }
+        rs = group_sum(rs, gmask);
         rho = make_double2(ar, ai);
-        res = warp_sum_f(rs);
-        if (fabs(res - thr) <= 1e-2 * thr) project64(rho, res);  // warp-uniform: res is a warp sum
+        res = rs;
+        if (fabsf(rs - (float)thr) <= 1e-2f * (float)thr) project64(rho, res);  // group-uniform
       } else {
         project64(rho, res);
       }
-      // ---- bin match: M_c^T k = digits of j (MSB first), lanes over the b digits
+      // ---- bin match: digit t of M_c^T k equals digit t of j (MSB first), digits over the group
       bool ok = true;
-      if (lane < b) {
+      {
         const int8_t* Mc = plan.i8 + job->off_M + (int64_t)c * n * b;
-        int dg = 0;
-        for (int i = 0; i < n; ++i) dg += (int)Mc[i * b + lane] * (int)kl[i];
-        int jr = jb;
-        for (int t = b - 1; t > lane; --t) jr /= q;
-        ok = (dg % q) == (jr % q);
-      }
-      const bool match = __all_sync(0xffffffffu, ok);
-      const bool single = match && !(res > thr);
-      if (single) {  // k, rho and the class for the record kernel
-        for (int w = lane; w < ks / 16; w += 32)
-          reinterpret_cast<uint4*>(plan.kbuf + gb * ks)[w] = reinterpret_cast<const uint4*>(kl)[w];
-        if (lane == 0) {
-          plan.rho[2 * gb] = rho.x;
-          plan.rho[2 * gb + 1] = rho.y;
+        for (int t = gi; t < b; t += DEC_G) {
+          int jr = jb;
+          for (int tt = b - 1; tt > t; --tt) jr /= q;
+          int dg = 0;
+          for (int i = 0; i < n; ++i) dg += (int)Mc[i * b + t] * (int)kl[i];
+          ok &= (dg % q) == (jr % q);
         }
       }
-      if (lane == 0) {
-        plan.bin_status[gb] = single ? 2 : 1;
-        atomicAdd(single ? &ctl->n_single : &ctl->n_multi, 1);
+      const bool match = (__ballot_sync(0xffffffffu, !ok) & gmask) == 0;
+      const bool single = match && !(res > thr);
+      if (active) {
+        if (single)  // k, rho and the class for the record kernel
+          for (int w = gi; w < ks / 16; w += DEC_G)
+            reinterpret_cast<uint4*>(plan.kbuf + gb * ks)[w] = reinterpret_cast<const uint4*>(kl)[w];
+        if (gi == 0) {
+          plan.bin_status[gb] = single ? 2 : 1;
+          if (single) {
+            plan.rho[2 * gb] = rho.x;
+            plan.rho[2 * gb + 1] = rho.y;
+          }
+          atomicAdd(single ? &ctl->n_single : &ctl->n_multi, 1);
+        }
       }
-      __syncwarp();
+      __syncwarp();  // the slot's buffers are reused by the next bin
     }
   }
 }
@@ -614,7 +653,7 @@ static int iteration(const qsft_plan* plan, int first, cudaStream_t st, cudaGrap
     scan_dirty_kernel<T><<<LIST_BLOCKS, SCAN_THREADS, 0, st>>>(*plan);
   }
   QSFT_CUDA_CHECK_LAUNCH();
-  decode_kernel<T><<<LIST_BLOCKS, WARPS_PER_BLOCK * 32, 0, st>>>(*plan);
+  decode_kernel<T><<<DEC_BLOCKS, DEC_THREADS, 0, st>>>(*plan);
   QSFT_CUDA_CHECK_LAUNCH();
   record_kernel<<<LIST_BLOCKS, SCAN_THREADS, 0, st>>>(*plan);
   QSFT_CUDA_CHECK_LAUNCH();
@@ -634,19 +673,20 @@ static int add_body(const qsft_plan* plan, cudaGraph_t body, cudaGraphConditiona
   void* a5[] = {&pl, &cond, &set, &mi};
   struct K {
     void* f;
-    unsigned grid, block;
+    unsigned grid, block, smem;
     void** args;
-  } ks[] = {{(void*)scan_dirty_kernel<T>, LIST_BLOCKS, SCAN_THREADS, a1},
-            {(void*)decode_kernel<T>, LIST_BLOCKS, WARPS_PER_BLOCK * 32, a1},
-            {(void*)record_kernel, LIST_BLOCKS, SCAN_THREADS, a1},
-            {(void*)peel_kernel<T>, LIST_BLOCKS, SCAN_THREADS, a1},
-            {(void*)iter_end_kernel, 1, 256, a5}};
+  } ks[] = {{(void*)scan_dirty_kernel<T>, LIST_BLOCKS, SCAN_THREADS, 0, a1},
+            {(void*)decode_kernel<T>, DEC_BLOCKS, DEC_THREADS, 0, a1},
+            {(void*)record_kernel, LIST_BLOCKS, SCAN_THREADS, 0, a1},
+            {(void*)peel_kernel<T>, LIST_BLOCKS, SCAN_THREADS, 0, a1},
+            {(void*)iter_end_kernel, 1, 256, 0, a5}};
   cudaGraphNode_t prev = nullptr;
   for (const K& k : ks) {
     cudaKernelNodeParams kp = {};
     kp.func = k.f;
     kp.gridDim = dim3(k.grid);
     kp.blockDim = dim3(k.block);
+    kp.sharedMemBytes = k.smem;
     kp.kernelParams = k.args;
     cudaGraphNode_t node;
     if (cudaGraphAddKernelNode(&node, body, prev ? &prev : nullptr, prev ? 1 : 0, &kp) != cudaSuccess)
