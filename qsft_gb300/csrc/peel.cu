@@ -20,7 +20,7 @@
 //                 :217, 247-255) and marks the ball detected in this iteration
 //                 keeping the largest (group, bin) -- the reference's dict
 //                 order, `ball_values` (:209-216).
-//   peel          thread per (detected ball, group l): subtract
+//   peel          per (detected ball, group l) -- a thread, or 8 for short lists: subtract
 //                 rho * omega^(D_l k) from bin M_l^T k (mod q) of group l
 //                 (qsft/qsft.py:223-241) and queue the changed bin for the
 //                 next scan.
@@ -217,11 +217,18 @@ constexpr int DEC_CPW = 32 / DEC_G;                    // bins per warp at a tim
 constexpr int DEC_BINS = DEC_THREADS / DEC_G;          // bins per block at a time
 constexpr int DEC_STAGE_RP = 64;
 constexpr int DEC_KB = QSFT_MAX_N + 16;
+constexpr int PEEL_THREAD_MIN = 1024;  // peel items of a job at least this many: one thread per item
 
 template <typename V>
 __device__ __forceinline__ V group_sum(V v, unsigned mask) {
 #pragma unroll
   for (int o = DEC_G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+  return v;
+}
+// the same over groups of g (a power of two <= 32) lanes, g chosen at run time
+template <typename V>
+__device__ __forceinline__ V group_sum_g(V v, unsigned mask, int g) {
+  for (int o = g >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
   return v;
 }
 
@@ -537,15 +544,20 @@ __device__ __forceinline__ void sub_entry(double2* p, double dx, double dy) {
   atomicAdd(&p->y, -dy);
 }
 
-// Thread per (ball detected in the iteration, group l): subtract
-// rho * omega^(<d_r, k>) from every row r of bin M_l^T k (mod q) of group l
-// and queue the bin for the next scan.  FP32 plans rotate rho in FP32: the
-// entries it is subtracted from are FP32.
+// Per (ball detected in the iteration, group l): each of the RP rows of bin
+// M_l^T k gets U -= rho * omega^(<d_r, k>) (one vector reduction) and the
+// changed bin is queued for the next scan once per iteration (stamped).  A
+// job's long list (the first iteration) takes one thread per item; a short
+// one takes DEC_G threads per item, digits and rows dealt over the group, to
+// cut the latency of each item when there are few to overlap.  FP32 plans
+// rotate rho in FP32 (the entries it is subtracted from are FP32).
 template <typename T>
 __global__ void __launch_bounds__(SCAN_THREADS) peel_kernel(qsft_plan plan) {
   if (__ldcg(plan.done_count) >= plan.njobs) return;  // every job has left the loop
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int gw = tid >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  __shared__ float2 s_w[33 * 32];                     // FP32 roots, loaded on first use
+  bool have_w = false;
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
   const int ks = plan.kstride;
   int64_t chunk0 = 0;
   for (int jid = 0; jid < plan.njobs; ++jid) {
@@ -554,7 +566,15 @@ __global__ void __launch_bounds__(SCAN_THREADS) peel_kernel(qsft_plan plan) {
     const qsft_job* __restrict__ job = plan.jobs + jid;
     const int C = job->C;
     const int cnt = ctl->n_unique * C;
-    const int nch = (cnt + 31) >> 5;
+    const int G = cnt >= PEEL_THREAD_MIN ? 1 : DEC_G, cpw = 32 / G, gi = lane % G;
+    if (G > 1 && !have_w) {  // uniform over the block: every thread sees the same counts
+      for (int i = threadIdx.x; i < 33 * 32; i += blockDim.x)
+        s_w[i] = make_float2((float)plan.roots[2 * i], (float)plan.roots[2 * i + 1]);
+      __syncthreads();
+      have_w = true;
+    }
+    const unsigned gmask = ((1u << G) - 1) << (lane - gi);
+    const int nch = (cnt + cpw - 1) / cpw;
     const int start = (int)(((int64_t)gw - chunk0) % nw + nw) % nw;
     chunk0 += nch;
     if (start >= nch) continue;
@@ -563,43 +583,84 @@ __global__ void __launch_bounds__(SCAN_THREADS) peel_kernel(qsft_plan plan) {
     const int iter = ctl->iter + 1;
     const int parity = iter & 1;
     const bool words_ok = (n & 3) == 0 && ((job->off_D & 3) == 0);
+    const float2* wq = s_w + q * 32;
     int32_t* list = plan.dirty + (int64_t)parity * plan.total_bins + job->off_bin;
-    for (int ch = start; ch < nch; ch += nw) {
-      const int it = ch * 32 + (tid & 31);
+    for (int ch = start; ch < nch; ch += nw) {   // uniform over the warp
+      const int it = ch * cpw + lane / G;
       bool fresh = false;
       int lb = 0;
-      if (it < cnt) {
-        const int u = it / C, l = it - (it / C) * C;
-        const int bid = __ldcg(plan.uniq + job->off_ball + u);
+      if (G == 1) {
+        if (it < cnt) {
+          const int u = it / C, l = it - (it / C) * C;
+          const int bid = __ldcg(plan.uniq + job->off_ball + u);
+          const int64_t gball = job->off_ball + bid;
+          const unsigned long long best = __ldcg(reinterpret_cast<const unsigned long long*>(plan.ball_best) + gball);
+          const int64_t gbest = job->off_bin + (int64_t)(best & 0xffffffffull);
+          const double2 rho = make_double2(__ldcg(plan.rho + 2 * gbest), __ldcg(plan.rho + 2 * gbest + 1));
+          const uint8_t* kl = plan.ball_k + gball * ks;  // written by the record kernel
+          const int8_t* Ml = plan.i8 + job->off_M + (int64_t)l * n * b;
+          int jl = 0;
+          for (int t = 0; t < b; ++t) {  // bin index, MSB-first digits of M_l^T k
+            int dg = 0;
+            for (int i = 0; i < n; ++i) dg += (int)Ml[i * b + t] * (int)kl[i];
+            jl = jl * q + dg % q;
+          }
+          c2<T>* Ul = reinterpret_cast<c2<T>*>(plan.U) + job->off_U + (int64_t)l * RP * B + jl;
+          const int8_t* Dl = plan.i8 + job->off_D + (int64_t)l * RP * n;
+          if (sizeof(T) == 4) {
+            const float rx = (float)rho.x, ry = (float)rho.y;
+            for (int r = 0; r < RP; ++r) {
+              const double2 w = root(plan.roots, q, row_phase(Dl + (int64_t)r * n, kl, n, words_ok, q));
+              const float wx = (float)w.x, wy = (float)w.y;
+              sub_entry(Ul + (int64_t)r * B, rx * wx - ry * wy, rx * wy + ry * wx);
+            }
+          } else {
+            for (int r = 0; r < RP; ++r) {
+              const double2 w = root(plan.roots, q, row_phase(Dl + (int64_t)r * n, kl, n, words_ok, q));
+              sub_entry(Ul + (int64_t)r * B, rho.x * w.x - rho.y * w.y, rho.x * w.y + rho.y * w.x);
+            }
+          }
+          lb = l * B + jl;
+          fresh = atomicExch(plan.bin_stamp + job->off_bin + lb, iter) != iter;
+        }
+      } else {
+        const bool active = it < cnt;
+        const int u = active ? it / C : 0, l = active ? it - (it / C) * C : 0;
+        const int bid = active ? __ldcg(plan.uniq + job->off_ball + u) : 0;
         const int64_t gball = job->off_ball + bid;
-        const unsigned long long best = __ldcg(reinterpret_cast<const unsigned long long*>(plan.ball_best) + gball);
-        const int64_t gbest = job->off_bin + (int64_t)(best & 0xffffffffull);
-        const double2 rho = make_double2(__ldcg(plan.rho + 2 * gbest), __ldcg(plan.rho + 2 * gbest + 1));
-        const uint8_t* kl = plan.ball_k + gball * ks;  // written by the record kernel
+        const uint8_t* kl = plan.ball_k + gball * ks;
         const int8_t* Ml = plan.i8 + job->off_M + (int64_t)l * n * b;
-        int jl = 0;
-        for (int t = 0; t < b; ++t) {  // bin index, MSB-first digits of M_l^T k
-          int dg = 0;
-          for (int i = 0; i < n; ++i) dg += (int)Ml[i * b + t] * (int)kl[i];
-          jl = jl * q + dg % q;
-        }
-        c2<T>* Ul = reinterpret_cast<c2<T>*>(plan.U) + job->off_U + (int64_t)l * RP * B + jl;
-        const int8_t* Dl = plan.i8 + job->off_D + (int64_t)l * RP * n;
-        if (sizeof(T) == 4) {
-          const float rx = (float)rho.x, ry = (float)rho.y;
-          for (int r = 0; r < RP; ++r) {
-            const double2 w = root(plan.roots, q, row_phase(Dl + (int64_t)r * n, kl, n, words_ok, q));
-            const float wx = (float)w.x, wy = (float)w.y;
-            sub_entry(Ul + (int64_t)r * B, rx * wx - ry * wy, rx * wy + ry * wx);
+        int part = 0;  // this thread's digits of the bin index
+        if (active)
+          for (int t = gi; t < b; t += G) {
+            int dg = 0;
+            for (int i = 0; i < n; ++i) dg += (int)Ml[i * b + t] * (int)kl[i];
+            int pw = 1;
+            for (int tt = t + 1; tt < b; ++tt) pw *= q;
+            part += (dg % q) * pw;
           }
-        } else {
-          for (int r = 0; r < RP; ++r) {
-            const double2 w = root(plan.roots, q, row_phase(Dl + (int64_t)r * n, kl, n, words_ok, q));
-            sub_entry(Ul + (int64_t)r * B, rho.x * w.x - rho.y * w.y, rho.x * w.y + rho.y * w.x);
+        const int jl = group_sum_g(part, gmask, G);
+        if (active) {
+          const unsigned long long best = __ldcg(reinterpret_cast<const unsigned long long*>(plan.ball_best) + gball);
+          const int64_t gbest = job->off_bin + (int64_t)(best & 0xffffffffull);
+          const double2 rho = make_double2(__ldcg(plan.rho + 2 * gbest), __ldcg(plan.rho + 2 * gbest + 1));
+          c2<T>* Ul = reinterpret_cast<c2<T>*>(plan.U) + job->off_U + (int64_t)l * RP * B + jl;
+          const int8_t* Dl = plan.i8 + job->off_D + (int64_t)l * RP * n;
+          if (sizeof(T) == 4) {
+            const float rx = (float)rho.x, ry = (float)rho.y;
+            for (int r = gi; r < RP; r += G) {
+              const float2 w = wq[row_phase(Dl + (int64_t)r * n, kl, n, words_ok, q)];
+              sub_entry(Ul + (int64_t)r * B, rx * w.x - ry * w.y, rx * w.y + ry * w.x);
+            }
+          } else {
+            for (int r = gi; r < RP; r += G) {
+              const double2 w = root(plan.roots, q, row_phase(Dl + (int64_t)r * n, kl, n, words_ok, q));
+              sub_entry(Ul + (int64_t)r * B, rho.x * w.x - rho.y * w.y, rho.x * w.y + rho.y * w.x);
+            }
           }
+          lb = l * B + jl;
+          if (gi == 0) fresh = atomicExch(plan.bin_stamp + job->off_bin + lb, iter) != iter;
         }
-        lb = l * B + jl;
-        fresh = atomicExch(plan.bin_stamp + job->off_bin + lb, iter) != iter;
       }
       const int pos = warp_append(fresh, jid, &ctl->n_dirty[parity]);  // once per bin per iteration
       if (fresh) list[pos] = lb;
