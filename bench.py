@@ -47,6 +47,10 @@ def parse():
     p.add_argument("--precision", default="fp32")
     p.add_argument("--seed", type=int, default=0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--serve-requests", type=int, default=10000, help="serving-mix requests (0: skip)")
+    p.add_argument("--serve-rate", type=float, default=0.0,
+                   help="Poisson arrival rate, requests/s (0: 80%% of the closed-loop capacity)")
+    p.add_argument("--serve-budget-gb", type=float, default=32.0)
     return p.parse_args()
 
 
@@ -139,12 +143,25 @@ def cpu_baseline(sample_rows=2, seed=0):
     return 1.0 / total, cores, sample
 
 
+def coef_nmse(keys, vals, req):
+    """||beta_hat - beta||^2 / ||beta||^2 over the union of the recovered and the
+    true support (by Parseval, the time-domain test NMSE of
+    qsft/test_helper.py:235-260 on the full domain)."""
+    true = {tuple(k): complex(a) for k, a in zip(req.locq.T.tolist(), req.strengths)}
+    est = {tuple(k): complex(a) for k, a in zip(keys.tolist(), vals)}
+    err = sum(abs(est.get(k, 0) - true.get(k, 0)) ** 2 for k in set(true) | set(est))
+    return float(err / sum(abs(a) ** 2 for a in true.values()))
+
+
+# DRAM bytes per launch from one ncu capture of this workload (dram__bytes_read.sum +
+# dram__bytes_write.sum; profiles/eval_gemm_q4n20b7_batch16.md, profiles/gwht_row_q4n20b7_batch16.md)
+NCU_TRAFFIC = {"eval": (35.0e6 + 203.6e6) + (13.8e6 + 13.4e6), "gwht": 348.4e6 + 203.1e6, "batch": 16}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    for _ in range(max(args.warmup, 0) and 1):
-        pass
     vals = []
     info = None
     for i in range(max(args.steps, 1)):
@@ -161,6 +178,72 @@ def run_reference(args):
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": info[0], "kind": "port", "sample": info[1]},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
+
+
+# ------------------------------------------------------------------ serving mix
+def run_serving(args, dev):
+    """The serving mix: `--serve-requests` requests drawn with q in {2,3,4,5,20},
+    n in [8,60], b in [3,8] (40 <= q^b <= 2^20), S in [10, min(2000, q^b/4)],
+    SNR in {10, 20, inf} dB, arriving as a Poisson process; admitted into
+    batches by device-memory footprint, up to 4 batches in flight.  Requests are
+    drawn before the clock starts.  FP64 plain = the same requests one at a
+    time in FP64 (a bounded sample)."""
+    import torch
+    from qsft_gb300.engine import Batch
+    from qsft_gb300.server import GpuExecutor, Server, poisson_arrivals, random_mix_request
+    N = args.serve_requests
+    np.random.seed(args.seed + 7)
+    t = time.perf_counter()
+    reqs = [random_mix_request() for _ in range(N)]
+    t_gen = time.perf_counter() - t
+    budget = int(args.serve_budget_gb * (1 << 30))
+    ex = GpuExecutor(max_inflight=4, device=dev)
+    srv = Server(ex, budget_bytes=budget, max_jobs=32, max_inflight=4)
+    srv.run(reqs[:128], np.zeros(128))                  # warm-up: allocator pool, kernel attributes
+    torch.cuda.synchronize()
+    ncal = min(N, 2000)
+    cal = srv.run(reqs[:ncal], np.zeros(ncal))          # closed loop: capacity
+    capacity = cal.completed() / cal.wall
+    rate = args.serve_rate if args.serve_rate > 0 else 0.8 * capacity
+    arr = poisson_arrivals(N, rate, np.random.RandomState(args.seed + 8))
+    rep = srv.run(reqs, arr)
+    torch.cuda.synchronize()
+    lat = rep.percentiles((50, 99))
+    sizes = [len(idx) for _, idx, _ in rep.batches]
+    # accuracy on the mix, by SNR class: NMSE against the true coefficients
+    by_snr = {}
+    for r, res in zip(reqs, rep.results):
+        if res is None:
+            continue
+        key = "inf" if r.noise_sd == 0 else "noisy"
+        by_snr.setdefault(key, []).append(coef_nmse(res.keys, res.values, r))
+    acc = {k: {"median": float(np.median(v)), "p99": float(np.percentile(v, 99)),
+               "frac_le_1e-4": float(np.mean(np.array(v) <= 1e-4))} for k, v in by_snr.items()}
+    # FP64 plain: one request at a time, eager, results read back
+    n64 = min(N, 200)
+    agree, t64 = 0, 0.0
+    for r, res in zip(reqs[:n64], rep.results[:n64]):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        b = Batch([r.spec()], precision="fp64", device=dev)
+        b.step()
+        k, v, _, _ = b.results(collected=True)[0]
+        t64 += time.perf_counter() - t
+        if res is not None and set(map(tuple, k.tolist())) == set(map(tuple, res.keys.tolist())):
+            agree += 1
+    fp64_tps = n64 / t64
+    tps = rep.completed() / rep.wall
+    return {"requests": N, "completed": rep.completed(), "failed": int(sum(e is not None for e in rep.errors)),
+            "arrival_rate": rate, "closed_loop_capacity": capacity, "throughput": tps, "unit": UNIT,
+            "wall_s": rep.wall, "latency_ms": {k: v * 1e3 for k, v in lat.items()},
+            "batches": len(rep.batches), "mean_batch": float(np.mean(sizes)) if sizes else 0.0,
+            "max_inflight": rep.max_inflight_seen, "peak_bytes": rep.peak_bytes, "budget_bytes": budget,
+            "fp64_plain": {"value": fp64_tps, "unit": UNIT, "sample": n64,
+                           "same_support_as_fp32_mix": f"{agree}/{n64}"},
+            "batched_fp32_over_fp64_plain": tps / fp64_tps,
+            "nmse_vs_truth": acc, "request_generation_s": t_gen,
+            "mix": "q{2,3,4,5,20} n[8,60] b[3,8] 40<=q^b<=2^20 S[10,min(2000,q^b/4)] SNR{10,20,inf}dB; "
+                   "noisy: NSO R=2, noiseless: identity R=1; C=3"}
 
 
 # ------------------------------------------------------------------ GPU
@@ -249,6 +332,7 @@ def run_ours(args):
     truth = [set(map(tuple, r.locq.T.tolist())) for r in reqs]
     found = [len(set(map(tuple, k.tolist())) & t) for (k, _, _, _), t in zip(res, truth)]
     iters = [int(c.iter) for (_, _, _, c) in res]
+    nmse32 = [coef_nmse(k, v, r) for (k, v, _, _), r in zip(res, reqs)]
 
     # ---- end to end through the public API, host buffers: a TransformStream
     # pipelines the steps (host packing / parsing of one batch overlaps the
@@ -302,6 +386,11 @@ def run_ours(args):
     z.record(stream)
     torch.cuda.synchronize()
     fp64_tps = n64 / (a.elapsed_time(z) / 1e3)
+    k64, v64, _, _ = b64.results(collected=True)[0]
+    nmse64 = coef_nmse(k64, v64, reqs[0])
+    same_support = set(map(tuple, k64.tolist())) == set(map(tuple, res[0][0].tolist()))
+
+    serving = run_serving(args, dev) if args.serve_requests > 0 else None
 
     if rank != 0:
         if world > 1:
@@ -333,12 +422,16 @@ def run_ours(args):
     gwht_bytes = 2.0 * samples * 8 * J
     roofline = {"kernel": "eval_cosets_gemm (operand + GEMM kernels)", "bound": "tensor",
                 "achieved": eval_flops / (e_ms / 1e3) / 1e12,
-                "peak": bf16, "unit": "TFLOP/s", "traffic": None,
+                "peak": bf16, "unit": "TFLOP/s",
+                "traffic": NCU_TRAFFIC["eval"] * J / NCU_TRAFFIC["batch"],
                 "peak_source": "measured" if "bf16_tflops" in peaks else "fallback",
                 "issued_tflops": None if issued is None else issued / (e_ms / 1e3) / 1e12}
     roofline["frac"] = roofline["achieved"] / roofline["peak"]
+    roofline["traffic_unit"] = "bytes per launch (ncu, prep + GEMM kernels)"
     roof_gwht = {"kernel": "gwht_row (transform + bin noise, one read and one write)", "bound": "hbm", "achieved": gwht_bytes / (g_ms / 1e3) / 1e9, "peak": hbm,
-                 "unit": "GB/s", "traffic": None, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
+                 "unit": "GB/s", "traffic": NCU_TRAFFIC["gwht"] * J / NCU_TRAFFIC["batch"],
+                 "algorithmic_bytes": gwht_bytes,
+                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
     roof_gwht["frac"] = roof_gwht["achieved"] / roof_gwht["peak"]
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -352,11 +445,18 @@ def run_ours(args):
                        "note": "batch completion latency through transform_batch"},
         "phase_ms": phase_ms,
         "fp64_plain": {"value": fp64_tps, "unit": UNIT, "batched_fp32_over_fp64_plain": value / fp64_tps},
-        "accuracy": {"true_support_found": f"{sum(found)}/{J * w['S']}", "iterations": iters[:8]},
+        "accuracy": {"true_support_found": f"{sum(found)}/{J * w['S']}", "iterations": iters[:8],
+                     "nmse_vs_truth_fp32": {"mean": float(np.mean(nmse32)), "max": float(np.max(nmse32))},
+                     "nmse_limit": 1e-4,
+                     "transform0": {"nmse_fp32_batched": nmse32[0], "nmse_fp64_plain": nmse64,
+                                    "nmse_rel_diff": abs(nmse32[0] - nmse64) / max(nmse64, 1e-300),
+                                    "same_support": bool(same_support)}},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "roofline": roofline, "roofline_gwht": roof_gwht, "clocks": clocks,
     }
+    if serving is not None:
+        line["serving_mix"] = serving
     if not args.no_cpu_baseline:
         v, cores, sample = cpu_baseline(sample_rows=2, seed=args.seed)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}

@@ -103,6 +103,17 @@ class JobSpec:
             raise ValueError("coded source needs a ReedSolomon description")
 
 
+def workspace_bytes(specs, precision="fp32"):
+    """Device bytes a :class:`Batch` of `specs` allocates (its workspace, inputs
+    and outputs; not the per-device roots table): the admission footprint of a
+    serving loop.  Host-only -- the library's layout functions, no GPU."""
+    b = Batch.__new__(Batch)
+    b.lib = load()
+    b.prec = precision_code(precision)
+    b._build_layout(list(specs))
+    return b.planned_bytes()
+
+
 def layout_key(spec):
     """Everything that fixes a job's place in the device workspace."""
     rs = (spec.rs.s, spec.rs.t) if spec.rs is not None else None
@@ -205,6 +216,40 @@ class Batch:
         self.gwht_rows_host = {k: np.concatenate(v) for k, v in rows.items()}
         self.gwht_meta_host = {k: np.concatenate(v).ravel() for k, v in meta.items()}
         self.max_iter = max(sp.max_iter for sp in specs)
+
+    def planned_bytes(self):
+        """Bytes ``_allocate`` takes for this layout, each buffer rounded up to the
+        caching allocator's 512-byte blocks."""
+        J, es = self.njobs, (8 if self.prec == QSFT_F32 else 16)
+        bins, slots, balls, ks = self.total_bins, self.total_slots, self.total_balls, self.kstride
+        cs = ctypes.sizeof(QsftCtrl) // 8
+        sizes = [max(self.n_i8, 1), max(self.n_a, 1) * es, max(self.n_u, 1) * es, ctypes.sizeof(QsftJob) * J,
+                 (J + 1) * 8, (J + 1) * 8, (J + 1) * 8, self.gf_host.size * 4,     # prefixes, GF tables
+                 bins * 16, bins * ks, slots * 8, balls * 8, balls * 4,             # rho, kbuf, ball table, best, uniq
+                 balls * ks, balls * 16, balls * 4,                                 # ball k, sum, count
+                 bins, bins * 4, 2 * bins * 4, bins * 4,                            # status, stamp, dirty, cand
+                 balls * ks, balls * 16, balls * 4, (2 + 2 * J + cs * J) * 8, 4]    # outputs, metadata, done
+        sizes += [8 * len(v) for v in self.gwht_rows_host.values()]
+        sizes += [4 * len(v) for v in self.gwht_meta_host.values()]
+        if self.prec == QSFT_F32:
+            p = QsftPlan()
+            index = (ctypes.c_int64 * (3 * J + 2))()
+            if self.lib.qsft_gemm_layout(self.jobs_host, J, ctypes.byref(p), index) == 0:
+                sizes += [max(int(p.gm_ws_bytes), 256), (3 * J + 2) * 8]
+        return int(sum((s + 511) // 512 * 512 for s in sizes))
+
+    def device_bytes(self):
+        """Bytes of this batch's device tensors (what ``planned_bytes`` predicts)."""
+        seen, total = {self.roots.untyped_storage().data_ptr()}, 0
+        for v in vars(self).values():
+            ts = v.values() if isinstance(v, dict) else [v]
+            for t in ts:
+                if isinstance(t, torch.Tensor) and t.device.type == "cuda":
+                    key = t.untyped_storage().data_ptr()
+                    if key not in seen:
+                        seen.add(key)
+                        total += (t.untyped_storage().nbytes() + 511) // 512 * 512
+        return total
 
     def _allocate(self):
         dev, J = self.device, self.njobs

@@ -18,7 +18,7 @@ import torch
 from .engine import MAX_ITER, Batch, JobSpec, layout_key
 from .query import get_Ms_and_Ds
 from .reed_solomon import ReedSolomon
-from .synthetic_signal import generate_signal_w
+from .synthetic_signal import draw_support
 
 
 class TransformRequest:
@@ -65,7 +65,7 @@ class TransformRequest:
 def random_request(q, n, b, S, C=3, R=2, snr_db=None, chan="nso", src="identity", t=None, a_min=1.0, a_max=10.0,
                    max_weight=None, noise_seed=None):
     """A seeded synthetic request drawn with the reference's generators (host numpy RNG)."""
-    _, locq, strengths = generate_signal_w(n, q, S, a_min, a_max, full=False, max_weight=max_weight)
+    locq, strengths = draw_support(n, q, S, a_min, a_max, max_weight=max_weight)
     qa = dict(query_method="complex", num_subsample=C, b=b, delays_method_source=src, delays_method_channel=chan,
               num_repeat=R, t=t)
     Ms, Ds = get_Ms_and_Ds(n, q, **qa)

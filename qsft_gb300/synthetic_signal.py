@@ -20,6 +20,16 @@ def generate_signal_w(n, q, sparsity, a_min, a_max, noise_sd=0, full=True, max_w
     """Random sparse transform, in the reference's RNG order
     (synt_exp/synt_src/synthetic_signal.py:10-38).  full=True is not supported
     (it materialises all q^n coefficients)."""
+    locq, strengths = draw_support(n, q, sparsity, a_min, a_max, max_weight)
+    if full:
+        raise NotImplementedError("full=True materialises q^n coefficients; use full=False")
+    signal_w = dict(zip(list(map(tuple, locq.T)), strengths))
+    return signal_w, locq, strengths
+
+
+def draw_support(n, q, sparsity, a_min, a_max, max_weight=None):
+    """The support (n x S, sorted) and coefficients of ``generate_signal_w``, drawn
+    in the same RNG order, without building the {k: a} dict."""
     max_weight = n if max_weight is None else max_weight
     if max_weight == n:
         locq = sort_qary_vecs(np.random.randint(q, size=(n, sparsity)).T).T
@@ -31,10 +41,7 @@ def generate_signal_w(n, q, sparsity, a_min, a_max, noise_sd=0, full=True, max_w
             locq[pos[i, :], i] = vals[:, i]
         locq = sort_qary_vecs(locq.T).T
     strengths = random_signal_strength_model(sparsity, a_min, a_max)
-    if full:
-        raise NotImplementedError("full=True materialises q^n coefficients; use full=False")
-    signal_w = dict(zip(list(map(tuple, locq.T)), strengths))
-    return signal_w, locq, strengths
+    return locq, strengths
 
 
 def get_random_subsampled_signal(n, q, noise_sd, sparsity, a_min, a_max, query_args, max_weight=None, **kw):
