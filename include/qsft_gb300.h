@@ -162,19 +162,21 @@ typedef struct qsft_plan {
   /* coset-factored tensor-core evaluation (qsft_eval_cosets_gemm); the gm_*
    * sizes and counts are filled in by qsft_gemm_layout                         */
   void* gm_ws;                 /* operand workspace of gm_ws_bytes                  */
-  const int64_t* gm_index;     /* [3*njobs+2]: CTA prefix [njobs+1] | operand-block
-                                * prefix [njobs+1] | byte offset of each job's
-                                * region in gm_ws [njobs]                            */
-  int64_t total_gm_work;       /* CTAs of the GEMM kernel                           */
+  const int64_t* gm_index;     /* [3*njobs+2]: work-unit prefix [njobs+1] |
+                                * operand-block prefix [njobs+1] | byte offset of
+                                * each job's region in gm_ws [njobs]                */
+  int64_t total_gm_work;       /* work units of the GEMM kernel (job, group, chunk
+                                * of delay rows, block of gm_mt*128 rows)           */
   int64_t total_gm_prep;       /* blocks of the operand kernel                      */
   int64_t gm_ws_bytes;
-  int32_t gm_mt;               /* 128-row MMA tiles per CTA (1, 2 or 4)             */
+  int32_t gm_mt;               /* 128-row MMA tiles per work unit (1 or 2)          */
   int32_t gm_kps;              /* K entries per support vector: 2 when every q is 2
                                 * or 4 (exact FP16 characters), else 4             */
   int32_t gm_nw;               /* 32-bit words of packed b-digit vectors (1, 2, 4)  */
-  int32_t gm_npmax;            /* largest N extent: 4*min(R*P, 64) rounded up to 16 */
+  int32_t gm_npmax;            /* largest N extent: 4 columns per delay row of a
+                                * chunk (<= 56 rows, equal chunks), rounded to 16   */
   int32_t gm_jt_bytes;         /* shared-memory bytes of the largest j table        */
-  int32_t gm_pad_;
+  int32_t gm_nacc;             /* accumulator buffers in tensor memory (1 or 2)     */
 } qsft_plan;
 
 /* tiles of 128 samples per tensor-core work item */
@@ -220,17 +222,19 @@ int qsft_eval_cosets_tc(const qsft_plan* plan, qsft_stream_t stream);
  * W the q^b x S character matrix of the j_s (exact in FP16 for q in {2, 4};
  * hi + lo FP16 halves otherwise) and C the S x R*P coefficient matrix (hi + lo
  * FP16 halves of a per-job power-of-two scaling, as separate N columns).  An operand kernel builds C
- * and the j_s into gm_ws; the GEMM kernel generates W tiles in shared memory
- * and runs tcgen05.mma kind::f16 into tensor memory.  U needs no zeroing.
+ * and the j_s into gm_ws; the persistent GEMM kernel (one CTA per SM) generates
+ * W tiles in tensor memory and runs tcgen05.mma kind::f16 into tensor-memory
+ * accumulators.  U needs no zeroing.
  * Needs the plan's gm_* fields from qsft_gemm_layout.
  */
 int qsft_eval_cosets_gemm(const qsft_plan* plan, qsft_stream_t stream);
 /*
  * Host-side sizing for qsft_eval_cosets_gemm: from the jobs' shapes (q, n, b,
- * C, R, P, S, B), fills plan->gm_mt, gm_kps, gm_nw, gm_npmax, gm_jt_bytes,
- * total_gm_work, total_gm_prep, gm_ws_bytes and index_host[3*njobs+2] (to be
- * uploaded to plan->gm_index).  A plan->gm_mt of 1 or 2 on entry caps the
- * 128-row tiles per CTA (default 4).  QSFT_ERR_TOO_LARGE when a job is outside the
+ * C, R, P, S, B), fills plan->gm_mt, gm_nacc, gm_kps, gm_nw, gm_npmax,
+ * gm_jt_bytes, total_gm_work, total_gm_prep, gm_ws_bytes and
+ * index_host[3*njobs+2] (to be uploaded to plan->gm_index).  A plan->gm_mt of 1
+ * on entry caps the 128-row tiles per work unit (default 2), a plan->gm_nacc of
+ * 1 keeps a single accumulator buffer (default: two when tensor memory allows).  QSFT_ERR_TOO_LARGE when a job is outside the
  * kernel's limits (q > 32, b > 16, R*P > 128, S > 8192): use
  * qsft_eval_cosets_tc for such batches.
  */

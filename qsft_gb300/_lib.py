@@ -86,7 +86,7 @@ class QsftPlan(ctypes.Structure):
         ("gm_ws", _P), ("gm_index", _P), ("total_gm_work", ctypes.c_int64), ("total_gm_prep", ctypes.c_int64),
         ("gm_ws_bytes", ctypes.c_int64), ("gm_mt", ctypes.c_int32), ("gm_kps", ctypes.c_int32),
         ("gm_nw", ctypes.c_int32), ("gm_npmax", ctypes.c_int32), ("gm_jt_bytes", ctypes.c_int32),
-        ("gm_pad_", ctypes.c_int32),
+        ("gm_nacc", ctypes.c_int32),
     ]
 
 

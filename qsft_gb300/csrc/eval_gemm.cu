@@ -36,14 +36,17 @@
 // from the row's digits (two dp4a per support vector for b <= 8) and issues
 // tcgen05.mma kind::f16 (M = 128, N, K = 16) into tensor memory.
 //
-// CTA: MT tiles of 128 rows (one producer thread per row, MT*128 threads),
-// one MMA-issuing warp and one bulk-copy warp.  A chunks and B chunks live in
-// two rings of their own (B deeper: its copies come from L2), each guarded by
-// mbarriers: afull (producer warps wrote A) / aempty (the MMAs that read it
-// completed), bfull (bulk copy landed) / bempty.  The producers then read the
-// MT accumulators back (tcgen05.ld) and store U directly.  Every wait is
-// bounded; on a timeout the CTA sets plan.status, drains its copies and MMAs
-// (bounded) and frees its tensor memory.
+// Work unit: MT tiles of 128 rows of one (job, group, chunk of delay rows).
+// The GEMM kernel is persistent (one CTA per SM over a cost-balanced range of
+// units) with four roles: producer warps (one thread per row) write A chunks
+// into a tensor-memory ring, one warp issues the MMAs, one warp streams the B
+// chunks into a shared-memory ring with bulk copies, and epilogue warps read the
+// accumulators back (tcgen05.ld) and store U.  Both rings and the one or two
+// accumulator buffers are guarded by mbarriers: afull (producers wrote A) /
+// aempty (the MMAs that read it completed), bfull (bulk copy landed) / bempty,
+// accf (a unit's MMAs completed) / acce (its accumulators were read).  Every
+// wait is bounded; on a timeout the CTA sets plan.status, drains its copies
+// and MMAs (bounded) and frees its tensor memory.
 #include "common.cuh"
 #include "tcgen05.cuh"
 
@@ -54,14 +57,13 @@ using namespace qsft::tc;
 constexpr int KC = 64;                     // K entries per stage: one 128-byte row (4 MMAs of K = 16)
 constexpr int TM = 128;                    // rows per MMA tile
 constexpr int HDR = 1024;                  // barriers, TMEM slot, flags, root table
-constexpr int MAX_MT = 4;
 constexpr int A_COLS = KC / 2;             // TMEM columns of one tile's A chunk (two FP16 per column)
-constexpr int NA = 2;                      // A stages (in tensor memory)
 constexpr int PREP_S = 32;                 // support vectors per operand block
-constexpr int REGION_HDR = 256;            // per-job header (inverse scale)
+constexpr int REGION_HDR = 256;            // per-job header (inverse scale; the first also the unit counter)
+constexpr int SCHED_OFF = 8;               // byte offset of the GEMM kernel's work-unit counter in gm_ws
 constexpr int MAX_SMEM = 227 * 1024;
 
-constexpr int RPC_MAX = 64;                // delay rows per N chunk (N = 4 columns each)
+constexpr int RPC_MAX = 56;                // delay rows per N chunk (N = 4 columns each, <= 224)
 
 struct Geo {
   int RPC, nch;      // delay rows per chunk, chunks
@@ -73,8 +75,8 @@ struct Geo {
 };
 __host__ __device__ inline Geo geo(int RP, int S, int kps, int nw) {
   Geo g;
-  g.RPC = RP < RPC_MAX ? RP : RPC_MAX;
-  g.nch = (RP + g.RPC - 1) / g.RPC;
+  g.nch = (RP + RPC_MAX - 1) / RPC_MAX;  // chunks of equal size (the last one at most one row shorter)
+  g.RPC = (RP + g.nch - 1) / g.nch;
   g.NP = (4 * g.RPC + 15) / 16 * 16;
   const int spc = KC / kps;
   g.S_pad = (S + spc - 1) / spc * spc;
@@ -166,6 +168,9 @@ __global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
   int ex = 0;
   if (mx > 0.f && isfinite(mx)) frexpf(mx, &ex);
   if (c == 0 && sb == 0 && tid == 0) *reinterpret_cast<float*>(region) = ldexpf(1.0f, ex - 14);
+  // the GEMM kernel's work-unit counter (header of the first region), reset before it runs
+  if (blockIdx.x == 0 && tid == 0)
+    *reinterpret_cast<unsigned long long*>(reinterpret_cast<unsigned char*>(plan.gm_ws) + SCHED_OFF) = 0ull;
   const float sc = ldexpf(1.0f, 14 - ex);
 
   // j table
@@ -231,54 +236,118 @@ __global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
 }
 
 // ---------------------------------------------------------------- GEMM
-constexpr int MAX_NB = 8;  // B stages (deeper: their bulk copies come from L2)
+// Persistent: one CTA per SM takes work units (job, group, chunk of delay
+// rows, block of MT*128 rows) from a global counter until none is left, so
+// units of unequal cost balance by themselves.  Its load warp takes them and
+// publishes them in a small shared-memory queue; every role reads the same
+// sequence from it:
+//   producers  (MT*4 warps)  A chunks of the row block into a TMEM ring
+//   epilogue   (MT*4 warps)  accumulators -> U, one 32-row quarter of one tile each
+//   MMA warp                 tcgen05.mma into accumulator buffer (unit % nacc)
+//   load warp                B chunks (bulk copies) into a shared-memory ring
+// The A and B rings run on across unit boundaries, so the next unit's operands
+// are staged while the epilogue drains the last one; with two accumulator
+// buffers (nacc = 2) its MMAs also overlap that drain.
+constexpr int MAX_NB = 8;   // B stages (deeper: their bulk copies come from L2)
+constexpr int MAX_NA = 4;   // A stages
+constexpr int TMEM_COLS = 512;
+constexpr int UQ = 8;       // queue of work units shared by the roles
+
+// A stages that fit beside nacc accumulator buffers of MT tiles x npmax columns
+__host__ __device__ inline int tmem_na(int mt, int nacc, int npmax) {
+  const int acc = (nacc * mt * npmax + 31) / 32 * 32;
+  const int na = (TMEM_COLS - acc) / (mt * A_COLS);
+  return na > MAX_NA ? MAX_NA : na;
+}
+
+struct Unit {
+  int j, c, h, q, b, S_pad, nK, NP, RP, rp0, nrp;
+  int64_t B, row0;
+  const unsigned char* region;  // the job's region (header: inverse scale)
+  const uint32_t* gJ;           // the group's j table
+  const unsigned char* gB;      // the chunk's B images
+  uint32_t CB;
+  float2* U;                    // samples of (job, group, first delay row of the chunk)
+};
 
 template <int KPS, int NW>
-__global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_plan plan, int nb) {
+__device__ __forceinline__ Unit decode_unit(const qsft_plan& plan, int64_t w, int nrows) {
+  Unit x;
+  const int nj = plan.njobs;
+  const int64_t* __restrict__ idx = plan.gm_index;
+  x.j = find_job(idx, nj, w);
+  const qsft_job* __restrict__ job = plan.jobs + x.j;
+  x.q = job->q;
+  x.b = job->b;
+  x.B = job->B;
+  x.RP = job->R * job->P;
+  const Geo g = geo(x.RP, job->S, KPS, NW);
+  const int64_t rblocks = (x.B + nrows - 1) / nrows;
+  const int64_t local = w - __ldg(idx + x.j);
+  const int ch = (int)(local / rblocks);
+  x.c = ch / g.nch;
+  x.h = ch - x.c * g.nch;
+  x.row0 = (local - (int64_t)ch * rblocks) * nrows;
+  x.rp0 = x.h * g.RPC;
+  x.nrp = min(g.RPC, x.RP - x.rp0);
+  x.nK = g.nK;
+  x.NP = g.NP;
+  x.S_pad = g.S_pad;
+  x.CB = g.CB;
+  x.region = reinterpret_cast<const unsigned char*>(plan.gm_ws) + __ldg(idx + 2 * (nj + 1) + x.j);
+  const unsigned char* gc = x.region + REGION_HDR + (int64_t)x.c * g.region_c;
+  x.gJ = reinterpret_cast<const uint32_t*>(gc);
+  x.gB = gc + g.jt_bytes + (int64_t)x.h * g.nK * g.CB;
+  x.U = reinterpret_cast<float2*>(plan.U) + job->off_U + ((int64_t)x.c * x.RP + x.rp0) * x.B;
+  return x;
+}
+
+
+// a ring position (slot, phase parity), advanced without division
+struct Ring {
+  uint32_t slot, phase, n;
+  __device__ __forceinline__ explicit Ring(uint32_t size) : slot(0), phase(0), n(size) {}
+  __device__ __forceinline__ void next() {
+    if (++slot == n) {
+      slot = 0;
+      phase ^= 1;
+    }
+  }
+};
+
+template <int KPS, int NW>
+__global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan plan, int nb) {
   extern __shared__ __align__(1024) unsigned char smem[];
-  uint64_t* bfull = reinterpret_cast<uint64_t*>(smem);  // [MAX_NB]
-  uint64_t* bempty = bfull + MAX_NB;                    // [MAX_NB]
-  uint64_t* afull = bempty + MAX_NB;                    // [NA]
-  uint64_t* aempty = afull + NA;                        // [NA]
-  uint64_t* accf = aempty + NA;
+  // chunk g (counted over the CTA's whole unit range) uses A slot g % NA and B slot g % nb
+  uint64_t* bfull = reinterpret_cast<uint64_t*>(smem);  // [MAX_NB] B chunk landed
+  uint64_t* cons = bfull + MAX_NB;                      // [MAX_NB] every MMA of chunk g (at g % nb) completed
+  uint64_t* afull = cons + MAX_NB;                      // [MAX_NA] A chunk written
+  uint64_t* accf = afull + MAX_NA;                      // [2] accumulator buffer written
+  uint64_t* acce = accf + 2;                            // [2] accumulator buffer drained
+  uint64_t* done = acce + 2;                            // every MMA issued has completed
+  uint64_t* uq_full = done + 1;                         // [UQ] unit index published
+  uint64_t* uq_empty = uq_full + UQ;                    // [UQ] every consumer warp has read it
+  uint64_t* pbar = uq_empty + UQ;                       // producer warps' group barrier
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 384);
   volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 388);
-  volatile int* n_con = reinterpret_cast<volatile int*>(smem + 392);
+  volatile uint32_t* n_con = reinterpret_cast<volatile uint32_t*>(smem + 392);
   uint2* qtab = reinterpret_cast<uint2*>(smem + 512);  // KPS = 4: (hi, lo) half2 words of omega^m
+  volatile long long* uq = reinterpret_cast<volatile long long*>(smem + 768);  // [UQ] unit indices, -1 ends
   uint32_t* jt = reinterpret_cast<uint32_t*>(smem + HDR);
-  const int MT = plan.gm_mt;
-  const uint32_t B_SLOT = (uint32_t)plan.gm_npmax * KC * 2;
+  const int MT = plan.gm_mt, nacc = plan.gm_nacc, npmax = plan.gm_npmax;
+  // A slots: what tensor memory holds beside the accumulators, and fewer than the
+  // B slots, so that a wait on cons[] for chunk g - NA cannot alias a later phase
+  const int NA = min(tmem_na(MT, nacc, npmax), nb - 1);
+  const uint32_t B_SLOT = (uint32_t)npmax * KC * 2;
   unsigned char* bring = smem + HDR + plan.gm_jt_bytes;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nprod = MT * TM;
-  const int mma_warp = nprod / 32, load_warp = mma_warp + 1;
+  const int epi_warp0 = nprod / 32, mma_warp = 2 * nprod / 32, load_warp = mma_warp + 1;
 
-  // ---- work item: (job, group, chunk of delay rows, block of MT*128 rows)
-  const int nj = plan.njobs;
-  const int64_t* __restrict__ idx = plan.gm_index;
-  const int64_t w = blockIdx.x;
-  const int j = find_job(idx, nj, w);
-  const qsft_job* __restrict__ job = plan.jobs + j;
-  const int q = job->q, b = job->b, B = job->B, S = job->S, RP = job->R * job->P;
-  const Geo g = geo(RP, S, KPS, NW);
-  const int64_t rblocks = (B + nprod - 1) / nprod;
-  const int64_t local = w - idx[j];
-  const int ch = (int)(local / rblocks);  // (group, chunk)
-  const int c = ch / g.nch, h = ch - (ch / g.nch) * g.nch;
-  const int64_t row0 = (local - (int64_t)ch * rblocks) * nprod;
-  const int rp0 = h * g.RPC, nrp = min(g.RPC, RP - rp0);
-  const unsigned char* region = reinterpret_cast<const unsigned char*>(plan.gm_ws) + idx[2 * (nj + 1) + j];
-  const unsigned char* gc = region + REGION_HDR + (int64_t)c * g.region_c;
-  const uint32_t* gJ = reinterpret_cast<const uint32_t*>(gc);
-  const unsigned char* gB = gc + g.jt_bytes + (int64_t)h * g.nK * g.CB;
-  float2* __restrict__ U = reinterpret_cast<float2*>(plan.U) + job->off_U + ((int64_t)c * RP + rp0) * B;
-
-  // ---- setup
-  // tensor memory: MT accumulators of NP columns, then NA stages of MT A tiles
-  const uint32_t acols = (uint32_t)(MT * g.NP + 31) / 32 * 32;
-  uint32_t ncols = 32;
-  while (ncols < acols + (uint32_t)(NA * MT * A_COLS)) ncols <<= 1;
+  // ---- setup: accumulators at column buf*MT*npmax + t*npmax, then NA slots of MT A tiles
+  const uint32_t acols = (uint32_t)(nacc * MT * npmax + 31) / 32 * 32;
+  const uint32_t ncols = TMEM_COLS;
   if (warp == mma_warp) {
     tmem_alloc(tmem_slot, ncols);
     tmem_relinquish();
@@ -286,202 +355,342 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
   if (tid == 0) {
     for (int i = 0; i < MAX_NB; ++i) {
       mbar_init(&bfull[i], 1);
-      mbar_init(&bempty[i], 1);
+      mbar_init(&cons[i], 1);
     }
-    for (int i = 0; i < NA; ++i) {
-      mbar_init(&afull[i], MT * 4);
-      mbar_init(&aempty[i], 1);
+    for (int i = 0; i < MAX_NA; ++i) mbar_init(&afull[i], MT * 4);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&accf[i], 1);
+      mbar_init(&acce[i], MT * 4);
     }
-    mbar_init(accf, 1);
-    // the swizzled layout needs 1024-byte aligned atoms
-    *abort_flag = (smem_u32(bring) & 1023u) ? 1 : 0;
+    mbar_init(done, 1);
+    for (int i = 0; i < UQ; ++i) {
+      mbar_init(&uq_full[i], 1);
+      mbar_init(&uq_empty[i], 2 * MT * 4 + 1);  // producer and epilogue warps, the MMA warp
+    }
+    mbar_init(pbar, MT * 4);
+    // the swizzled layout needs 1024-byte aligned atoms; the TMEM plan must fit
+    *abort_flag = ((smem_u32(bring) & 1023u) || NA < 2 || nb > MAX_NB || (MT != 1 && MT != 2) ||
+                   (nacc != 1 && nacc != 2)) ? 1 : 0;
     *n_con = 0;
     fence_mbar_init();
   }
-  if (KPS == 4 && tid < q) {
-    const double* r = plan.roots + ((int64_t)q * 32 + tid) * 2;
-    const float wr = (float)r[0], wi = (float)r[1];
-    const __half hr = __float2half_rn(wr), hi = __float2half_rn(wi);
-    qtab[tid] = make_uint2(h2_bits(hr, hi), h2_bits(__float2half_rn(wr - __half2float(hr)),
-                                                    __float2half_rn(wi - __half2float(hi))));
-  }
-  for (int i = tid; i < g.S_pad * NW; i += blockDim.x) jt[i] = __ldg(gJ + i);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const int nK = g.nK;
-  int iss = 0;  // bulk copies issued (load warp, lane 0)
+  uint32_t iss = 0;  // bulk copies issued (load warp, lane 0)
+  // next unit of a consumer warp (-1: no more, or a wait gave up); lane 0 takes
+  // it from the queue and frees the slot at once
+  auto next_unit = [&](Ring& r) -> long long {
+    long long u = -1;
+    if (lane == 0) {
+      if (mbar_wait(&uq_full[r.slot], r.phase)) {
+        u = uq[r.slot];
+      } else {
+        *abort_flag = 1;
+      }
+      mbar_arrive(&uq_empty[r.slot]);
+    }
+    r.next();
+    return __shfl_sync(~0u, u, 0);
+  };
 
   if (tid < nprod) {
-    // ---- producers: one row of A per thread
-    const int t = tid >> 7, tr = tid & (TM - 1);
-    const int64_t l = row0 + tid;
-    uint32_t lw[NW];
+    // ---- producers: one row of A per thread, for every unit of the range
+    const int t = tid >> 7;
+    const uint32_t a_lane = tmem + ((uint32_t)(warp & 3) * 32 << 16) + acols + (uint32_t)t * A_COLS;
+    int cur_j = -1, cur_c = -1;
+    Ring fa((uint32_t)NA);   // A slot of chunk g
+    Ring ce((uint32_t)nb);   // cons[] position of chunk g - NA
+    Ring uqr(UQ);
+    uint32_t g = 0, pph = 0;
+    // the producer warps' group barrier (bounded): every producer thread's shared
+    // stores before it are visible to every producer thread after it
+    auto group_sync = [&]() {
+      __threadfence_block();
+      __syncwarp();
+      int ok = 1;
+      if (lane == 0) {
+        mbar_arrive(pbar);
+        ok = mbar_wait(pbar, pph);
+        if (!ok) *abort_flag = 1;
+      }
+      pph ^= 1;
+      __syncwarp();
+    };
+    for (;;) {
+      const long long u = next_unit(uqr);
+      if (u < 0) break;
+      const Unit x = decode_unit<KPS, NW>(plan, u, nprod);
+      if (x.j != cur_j || x.c != cur_c) {  // the group's j table (and q's roots) into shared memory
+        group_sync();                      // every producer is done with the previous table
+        for (int i = tid; i < x.S_pad * NW; i += nprod) jt[i] = __ldg(x.gJ + i);
+        if (KPS == 4 && tid < x.q) {
+          const double* r = plan.roots + ((int64_t)x.q * 32 + tid) * 2;
+          const float wr = (float)r[0], wi = (float)r[1];
+          const __half hr = __float2half_rn(wr), hi = __float2half_rn(wi);
+          qtab[tid] = make_uint2(h2_bits(hr, hi), h2_bits(__float2half_rn(wr - __half2float(hr)),
+                                                          __float2half_rn(wi - __half2float(hi))));
+        }
+        group_sync();
+        cur_j = x.j;
+        cur_c = x.c;
+      }
+      if (*abort_flag) continue;  // keep taking units until the queue ends
+      const int64_t l = x.row0 + tid;
+      uint32_t lw[NW];
 #pragma unroll
-    for (int k = 0; k < NW; ++k) lw[k] = 0;
-    if (l < B) {
-      uint32_t v = (uint32_t)l;
+      for (int k = 0; k < NW; ++k) lw[k] = 0;
+      if (l < x.B) {
+        uint32_t v = (uint32_t)l;
 #pragma unroll
-      for (int d = 4 * NW - 1; d >= 0; --d) {  // MSB-first digits: digit b-1 is l mod q
-        if (d < b) {
-          const uint32_t qt = v / (uint32_t)q;
-          lw[d >> 2] |= (v - qt * (uint32_t)q) << (8 * (d & 3));
-          v = qt;
+        for (int d = 4 * NW - 1; d >= 0; --d) {  // MSB-first digits: digit b-1 is l mod q
+          if (d < x.b) {
+            const uint32_t qt = v / (uint32_t)x.q;
+            lw[d >> 2] |= (v - qt * (uint32_t)x.q) << (8 * (d & 3));
+            v = qt;
+          }
         }
       }
+      const ModQ mq = make_modq(x.q);
+      // the store of slot `pend` is still in flight while the next chunk is
+      // computed; its afull is signalled once the store has completed
+      int pend = -1;
+      for (int kc = 0; kc < x.nK; ++kc) {
+        const int s0 = kc * (KC / KPS);
+        uint32_t av[32];  // the row's 64 FP16 entries of this chunk, K order
+        if constexpr (KPS == 2) {
+          // four support vectors per 16-byte chunk; omega_4^m as half2 (re, im):
+          // high bytes from the tables 0x00BC003C (re) and 0xBC003C00 (im), low bytes zero
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const uint32_t* jp = jt + (s0 + 4 * i) * NW;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+              uint32_t d = 0;
+#pragma unroll
+              for (int k = 0; k < NW; ++k) d = __dp4a(lw[k], jp[e * NW + k], d);
+              av[4 * i + e] = __byte_perm(0x00BC003Cu, 0xBC003C00u, 0x4101u + (d & 3u) * 0x1010u);
+            }
+          }
+        } else {
+          // two support vectors per chunk: (hi, lo) half2 words of omega^m
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            const uint32_t* jp = jt + (s0 + 2 * i) * NW;
+            uint32_t d0 = 0, d1 = 0;
+#pragma unroll
+            for (int k = 0; k < NW; ++k) {
+              d0 = __dp4a(lw[k], jp[k], d0);
+              d1 = __dp4a(lw[k], jp[NW + k], d1);
+            }
+            const uint2 h0 = qtab[modq(d0, mq)], h1 = qtab[modq(d1, mq)];
+            av[4 * i] = h0.x;
+            av[4 * i + 1] = h0.y;
+            av[4 * i + 2] = h1.x;
+            av[4 * i + 3] = h1.y;
+          }
+        }
+        if (pend >= 0) {
+          tmem_st_wait();
+          tc_fence_before();
+          __syncwarp();
+          if (lane == 0) mbar_arrive(&afull[pend]);
+          pend = -1;
+        }
+        if (g >= (uint32_t)NA) {  // slot reuse: the MMAs of chunk g - NA have completed
+          int go = 1;
+          if (lane == 0) go = !*abort_flag && mbar_wait(&cons[ce.slot], ce.phase);
+          go = __shfl_sync(~0u, go, 0);
+          if (!go) {
+            if (lane == 0) *abort_flag = 1;
+            break;
+          }
+          ce.next();
+        }
+        tmem_st32(a_lane + fa.slot * (uint32_t)(MT * A_COLS), av);
+        pend = (int)fa.slot;
+        fa.next();
+        ++g;
+      }
+      if (pend >= 0) {
+        tmem_st_wait();
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&afull[pend]);
+      }
     }
-    const ModQ mq = make_modq(q);
-    // this warp's TMEM lanes (its 32 rows of tile t) and the tile's A columns
-    const uint32_t a_lane = tmem + ((uint32_t)(warp & 3) * 32 << 16) + acols + (uint32_t)t * A_COLS;
-    (void)tr;
-    for (int kc = 0; kc < nK; ++kc) {
-      const int st = kc % NA;
-      const uint32_t ph = (uint32_t)(kc / NA) & 1;
-      int go = 1;
-      if (lane == 0) go = !*abort_flag && mbar_wait(&aempty[st], ph ^ 1);
-      go = __shfl_sync(~0u, go, 0);
-      if (!go) {
+  } else if (warp < mma_warp) {
+    // ---- epilogue: tile et, rows lq*32 + lane of it
+    const int et = (warp - epi_warp0) >> 2, lq = warp & 3;
+    Ring ac((uint32_t)nacc), uqr(UQ);
+    for (;;) {
+      const long long u = next_unit(uqr);
+      if (u < 0) break;
+      int ok = 1;
+      if (lane == 0) ok = !*abort_flag && mbar_wait_sleep(&accf[ac.slot], ac.phase);
+      ok = __shfl_sync(~0u, ok, 0);
+      if (!ok) {
         if (lane == 0) *abort_flag = 1;
         break;
       }
-      const int s0 = kc * (KC / KPS);
-      uint32_t av[32];  // the row's 64 FP16 entries of this stage, K order
-      if constexpr (KPS == 2) {
-        // four support vectors per 16-byte chunk; omega_4^m as half2 (re, im):
-        // high bytes from the tables 0x00BC003C (re) and 0xBC003C00 (im), low bytes zero
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const uint32_t* jp = jt + (s0 + 4 * i) * NW;
-          uint32_t wv[4];
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            uint32_t d = 0;
-#pragma unroll
-            for (int k = 0; k < NW; ++k) d = __dp4a(lw[k], jp[u * NW + k], d);
-            wv[u] = __byte_perm(0x00BC003Cu, 0xBC003C00u, 0x4101u + (d & 3u) * 0x1010u);
-          }
-#pragma unroll
-          for (int u = 0; u < 4; ++u) av[4 * i + u] = wv[u];
-        }
-      } else {
-        // two support vectors per chunk: (hi, lo) half2 words of omega^m
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const uint32_t* jp = jt + (s0 + 2 * i) * NW;
-          uint32_t d0 = 0, d1 = 0;
-#pragma unroll
-          for (int k = 0; k < NW; ++k) {
-            d0 = __dp4a(lw[k], jp[k], d0);
-            d1 = __dp4a(lw[k], jp[NW + k], d1);
-          }
-          const uint2 h0 = qtab[modq(d0, mq)], h1 = qtab[modq(d1, mq)];
-          av[4 * i] = h0.x;
-          av[4 * i + 1] = h0.y;
-          av[4 * i + 2] = h1.x;
-          av[4 * i + 3] = h1.y;
-        }
-      }
-      tmem_st32(a_lane + (uint32_t)(st * MT * A_COLS), av);
-      tmem_st_wait();
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&afull[st]);
-    }
-    // ---- epilogue: accumulators -> U
-    int ok = 1;
-    if (lane == 0) ok = mbar_wait(accf, 0) && !*abort_flag;
-    ok = __shfl_sync(~0u, ok, 0);
-    tc_fence_after();
-    if (ok) {
-      const int lq = warp & 3;
-      const int64_t row = row0 + t * TM + lq * 32 + lane;
-      const bool live = row < B;
-      const uint32_t tb = tmem + ((uint32_t)(lq * 32) << 16) + (uint32_t)(t * g.NP);
-      float2* __restrict__ ur = U + row;
-      const float inv = *reinterpret_cast<const float*>(region);
-      const int ng = g.NP / 16;
+      tc_fence_after();
+      const Unit x = decode_unit<KPS, NW>(plan, u, nprod);
+      const int64_t row = x.row0 + et * TM + lq * 32 + lane;
+      const bool live = row < x.B;
+      const uint32_t tb = tmem + ((uint32_t)(lq * 32) << 16) + ac.slot * (uint32_t)(MT * npmax) + (uint32_t)(et * npmax);
+      float2* __restrict__ ur = x.U + row;
+      const float inv = *reinterpret_cast<const float*>(x.region);
+      const int ng = x.NP / 16;
+      const int nrp = x.nrp;
+      const int64_t B = x.B;
       // 16 columns = 4 delay rows x (re hi, re lo, im hi, im lo)
       auto emit = [&](const uint32_t(&r)[16], int cg) {
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-          const int rp = cg * 4 + i;
+        for (int k = 0; k < 4; ++k) {
+          const int rp = cg * 4 + k;
           if (live && rp < nrp)
             ur[(int64_t)rp * B] =
-                make_float2((__uint_as_float(r[4 * i]) + __uint_as_float(r[4 * i + 1])) * inv,
-                            (__uint_as_float(r[4 * i + 2]) + __uint_as_float(r[4 * i + 3])) * inv);
+                make_float2((__uint_as_float(r[4 * k]) + __uint_as_float(r[4 * k + 1])) * inv,
+                            (__uint_as_float(r[4 * k + 2]) + __uint_as_float(r[4 * k + 3])) * inv);
         }
       };
-      uint32_t ra[16], rb[16];
-      tmem_ld16(tb, ra);
-      for (int cg = 0; cg < ng; cg += 2) {
-        tmem_ld_wait_regs(ra);
-        if (cg + 1 < ng) tmem_ld16(tb + (cg + 1) * 16, rb);
-        emit(ra, cg);
-        if (cg + 1 < ng) {
-          tmem_ld_wait_regs(rb);
-          if (cg + 2 < ng) tmem_ld16(tb + (cg + 2) * 16, ra);
-          emit(rb, cg + 1);
-        }
+      // rounds of three 16-column loads and one wait (a wait covers every load in flight)
+      for (int cg0 = 0; cg0 < ng; cg0 += 3) {
+        uint32_t r0[16], r1[16], r2[16];
+        tmem_ld16(tb + cg0 * 16, r0);
+        if (cg0 + 1 < ng) tmem_ld16(tb + (cg0 + 1) * 16, r1);
+        if (cg0 + 2 < ng) tmem_ld16(tb + (cg0 + 2) * 16, r2);
+        tmem_ld_wait_regs(r0);
+        tmem_ld_wait_regs(r1);
+        tmem_ld_wait_regs(r2);
+        emit(r0, cg0);
+        if (cg0 + 1 < ng) emit(r1, cg0 + 1);
+        if (cg0 + 2 < ng) emit(r2, cg0 + 2);
       }
-    } else if (lane == 0) {
-      *abort_flag = 1;
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&acce[ac.slot]);
+      ac.next();
     }
   } else if (warp == mma_warp) {
-    // ---- MMA issue.  Descriptors differ between stages, tiles and K steps
+    // ---- MMA issue.  Descriptors differ between slots, tiles and K steps
     // only in the start-address field (smem address >> 4 < 2^14, no carry),
     // so they are built once and offset.
     if (lane == 0) {
-      const uint32_t idesc = tc::make_idesc(TM, g.NP);
       const uint64_t b0 = desc_sw128(smem_u32(bring));
-      int con = 0;
-      for (int kc = 0; kc < nK; ++kc) {
-        const int sa = kc % NA, sbi = kc % nb;
-        if (*abort_flag) break;
-        if (!mbar_wait(&bfull[sbi], (uint32_t)(kc / nb) & 1) || !mbar_wait(&afull[sa], (uint32_t)(kc / NA) & 1)) {
+      Ring fa((uint32_t)NA), fb((uint32_t)nb), ac((uint32_t)nacc), uqr(UQ);
+      uint32_t g = 0;
+      for (;;) {
+        long long u = -1;  // lane 0 alone runs this loop: the queue without a shuffle
+        if (mbar_wait(&uq_full[uqr.slot], uqr.phase)) u = uq[uqr.slot]; else *abort_flag = 1;
+        mbar_arrive(&uq_empty[uqr.slot]);
+        uqr.next();
+        if (u < 0 || *abort_flag) break;
+        const Unit x = decode_unit<KPS, NW>(plan, u, nprod);
+        if (!mbar_wait(&acce[ac.slot], ac.phase ^ 1)) {
           *abort_flag = 1;
           break;
         }
         tc_fence_after();
-        const uint32_t ad = tmem + acols + (uint32_t)(sa * MT * A_COLS);
-        const uint64_t bd = b0 + ((sbi * B_SLOT) >> 4);
-        for (int t = 0; t < MT; ++t) {
-          const uint32_t dt = tmem + (uint32_t)(t * g.NP);
-          const uint32_t at = ad + (uint32_t)(t * A_COLS);
+        const uint32_t idesc = tc::make_idesc(TM, x.NP);
+        const uint32_t dbase = tmem + ac.slot * (uint32_t)(MT * npmax);
+        bool ok = true;
+        for (int kc = 0; kc < x.nK; ++kc) {
+          // both operands of chunk g: one non-blocking test each, issued together;
+          // the bounded blocking waits only when either is not there yet
+          const bool rb = mbar_test_wait(&bfull[fb.slot], fb.phase);
+          const bool ra = mbar_test_wait(&afull[fa.slot], fa.phase);
+          if (!(rb && ra) && (*abort_flag || !mbar_wait(&bfull[fb.slot], fb.phase) ||
+                               !mbar_wait(&afull[fa.slot], fa.phase))) {
+            ok = false;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t ad = tmem + acols + fa.slot * (uint32_t)(MT * A_COLS);
+          const uint64_t bd = b0 + ((fb.slot * B_SLOT) >> 4);
+          for (int t = 0; t < MT; ++t) {
+            const uint32_t dt = dbase + (uint32_t)(t * npmax);
+            const uint32_t at = ad + (uint32_t)(t * A_COLS);
 #pragma unroll
-          for (int ks = 0; ks < KC / 16; ++ks)  // K = 16 is 32 bytes along the swizzled row
-            mma_f16_ts(dt, at + ks * 8, bd + ks * 2, idesc, (kc | ks) > 0);
+            for (int ks = 0; ks < KC / 16; ++ks)  // K = 16 is 32 bytes along the swizzled row
+              mma_f16_ts(dt, at + ks * 8, bd + ks * 2, idesc, (kc | ks) > 0);
+          }
+          mma_commit(&cons[fb.slot]);  // frees A slot and B slot of chunk g
+          fa.next();
+          fb.next();
+          ++g;
         }
-        mma_commit(&aempty[sa]);
-        mma_commit(&bempty[sbi]);
-        con = kc + 1;
-      }
-      mma_commit(accf);  // arrives once every MMA issued above has completed
-      *n_con = con;
-    }
-    __syncwarp();
-  } else if (warp == load_warp) {
-    // ---- B chunks: one bulk copy per stage, up to nb in flight
-    if (lane == 0) {
-      for (int kc = 0; kc < nK; ++kc) {
-        const int st = kc % nb;
-        if (*abort_flag) break;
-        if (!mbar_wait(&bempty[st], ((uint32_t)(kc / nb) & 1) ^ 1)) {
+        if (!ok) {
           *abort_flag = 1;
           break;
         }
-        mbar_arrive_expect_tx(&bfull[st], g.CB);
-        bulk_g2s(bring + st * B_SLOT, gB + (int64_t)kc * g.CB, g.CB, &bfull[st]);
-        iss = kc + 1;
+        mma_commit(&accf[ac.slot]);  // arrives when every MMA of the unit has completed
+        ac.next();
       }
+      *n_con = g;
+      mma_commit(done);  // arrives once every MMA issued above has completed
+      if (!mbar_wait(done, 0)) *abort_flag = 1;
+    }
+    __syncwarp();
+  } else if (warp == load_warp) {
+    // ---- B chunks: one bulk copy per slot, up to nb in flight, across units
+    if (lane == 0) {
+      // also the scheduler: takes units from the global counter (reset by the
+      // operand kernel) and publishes them, one unit ahead of its own copies
+      unsigned long long* counter =
+          reinterpret_cast<unsigned long long*>(reinterpret_cast<unsigned char*>(plan.gm_ws) + SCHED_OFF);
+      const long long total = plan.total_gm_work;
+      Ring fb((uint32_t)nb), uqw(UQ);
+      bool ended = false;
+      // one unit per take: units of unequal cost balance by themselves and the
+      // tail is a single unit (runs of consecutive units measured slower)
+      auto take = [&]() -> long long {
+        const long long u = (long long)atomicAdd(counter, 1ull);
+        return u < total ? u : -1;
+      };
+      auto publish = [&](bool stop) -> long long {
+        if (ended) return -1;
+        if (!mbar_wait(&uq_empty[uqw.slot], uqw.phase ^ 1)) {
+          *abort_flag = 1;
+          ended = true;
+          return -1;
+        }
+        const long long u = stop ? -1 : take();
+        uq[uqw.slot] = u;
+        mbar_arrive(&uq_full[uqw.slot]);  // release: the index is visible with the phase
+        uqw.next();
+        if (u < 0) ended = true;
+        return u;
+      };
+      uint32_t g = 0;
+      long long cur = publish(false);
+      long long ahead = cur >= 0 ? publish(false) : -1;
+      while (cur >= 0) {
+        const Unit x = decode_unit<KPS, NW>(plan, cur, nprod);
+        for (int kc = 0; kc < x.nK; ++kc) {
+          // slot reuse: the MMAs of chunk g - nb have completed (the first round passes)
+          if (*abort_flag || !mbar_wait(&cons[fb.slot], fb.phase ^ 1)) {
+            *abort_flag = 1;
+            break;
+          }
+          mbar_arrive_expect_tx(&bfull[fb.slot], x.CB);
+          bulk_g2s(bring + fb.slot * B_SLOT, x.gB + (int64_t)kc * x.CB, x.CB, &bfull[fb.slot]);
+          fb.next();
+          iss = ++g;
+        }
+        if (*abort_flag) break;
+        cur = ahead;
+        ahead = cur >= 0 ? publish(false) : -1;
+      }
+      publish(true);  // ends the queue for every consumer (after an abort too)
     }
     __syncwarp();
   }
   __syncthreads();  // every role loop has ended; n_con is final
   if (warp == load_warp && lane == 0)
-    for (int kc = *n_con; kc < iss; ++kc)  // copies that no MMA consumed: let them land (bounded)
-      mbar_wait(&bfull[kc % nb], (uint32_t)(kc / nb) & 1);
-  if (warp == mma_warp && lane == 0 && *abort_flag) mbar_wait(accf, 0);  // MMAs done before dealloc
+    for (uint32_t k = *n_con; k < iss; ++k)  // copies that no MMA consumed: let them land (bounded)
+      mbar_wait(&bfull[k % (uint32_t)nb], (k / (uint32_t)nb) & 1);
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -489,11 +698,10 @@ __global__ void __launch_bounds__(MAX_MT * TM + 64, 1) eval_gemm_kernel(qsft_pla
   if (warp == mma_warp) tmem_dealloc(tmem, ncols);
 }
 
-// stage counts for the shared-memory budget: 4 A + 8 B stages, B first trimmed to 4
-// B stages for the shared-memory budget (A lives in tensor memory)
+// B slots for the shared-memory budget (A lives in tensor memory)
 inline bool pick_stages(int npmax, int jt_bytes, int& nb, int& smem) {
   const int fixed = HDR + jt_bytes, bb = npmax * KC * 2;
-  for (nb = MAX_NB; nb >= 2; --nb)
+  for (nb = MAX_NB; nb >= 3; --nb)  // at least 3: the A ring keeps 2 slots below it
     if (fixed + nb * bb <= MAX_SMEM) {
       smem = fixed + nb * bb;
       return true;
@@ -511,7 +719,11 @@ static int launch(const qsft_plan* p, cudaStream_t st) {
   }
   auto kern = eval_gemm_kernel<KPS, NW>;
   if (!ensure_smem((const void*)kern, smem)) return QSFT_ERR_CUDA;
-  kern<<<(unsigned)p->total_gm_work, p->gm_mt * TM + 64, smem, st>>>(*p, nb);
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return QSFT_ERR_CUDA;
+  const int64_t grid = p->total_gm_work < sms ? p->total_gm_work : sms;  // persistent: one CTA per SM
+  kern<<<(unsigned)grid, 2 * p->gm_mt * TM + 64, smem, st>>>(*p, nb);
   QSFT_CUDA_CHECK_LAUNCH();
   return QSFT_OK;
 }
@@ -550,10 +762,20 @@ extern "C" int qsft_gemm_layout(const qsft_job* jobs, int njobs, qsft_plan* plan
     const gm::Geo g = gm::geo(jobs[i].R * jobs[i].P, jobs[i].S, kps, nw);
     npmax = npmax > g.NP ? npmax : g.NP;
   }
-  int mt = (plan->gm_mt == 1 || plan->gm_mt == 2) ? plan->gm_mt : gm::MAX_MT;
-  // tensor memory: accumulators (32-column aligned) + NA stages of A tiles <= 512 columns
-  while (mt > 1 && ((mt * npmax + 31) / 32 * 32 + gm::NA * mt * gm::A_COLS > 512 || (int64_t)(mt / 2) * gm::TM >= maxB))
-    mt /= 2;
+  // tensor memory: nacc accumulator buffers of mt tiles + at least two A slots.
+  // Preference: the larger mt (a B chunk feeds more rows, and the MMA warp's
+  // per-chunk waits and commit cover twice the MMAs), then two buffers (the
+  // epilogue overlaps the next unit's MMAs).  Presets cap both.
+  const int mt_cap = (plan->gm_mt == 1 || plan->gm_mt == 2) ? plan->gm_mt : 2;
+  const int nacc_cap = plan->gm_nacc == 1 ? 1 : 2;
+  int mt = 0, nacc = 0;
+  for (int m = mt_cap; m >= 1 && !mt; --m)
+    for (int na_ = nacc_cap; na_ >= 1 && !mt; --na_)
+      if ((m == 1 || (int64_t)(m / 2) * gm::TM < maxB) && gm::tmem_na(m, na_, npmax) >= 2) {
+        mt = m;
+        nacc = na_;
+      }
+  if (!mt) return QSFT_ERR_TOO_LARGE;
   int64_t work = 0, prep = 0, off = 0;
   index[0] = 0;
   index[njobs + 1] = 0;
@@ -574,6 +796,7 @@ extern "C" int qsft_gemm_layout(const qsft_job* jobs, int njobs, qsft_plan* plan
   if (!gm::pick_stages(npmax, jt, nb, smem)) return QSFT_ERR_TOO_LARGE;
   if (work > 0x7fffffffLL || prep > 0x7fffffffLL) return QSFT_ERR_TOO_LARGE;
   plan->gm_mt = mt;
+  plan->gm_nacc = nacc;
   plan->gm_kps = kps;
   plan->gm_nw = nw;
   plan->gm_npmax = npmax;
@@ -589,8 +812,9 @@ extern "C" int qsft_eval_cosets_gemm(const qsft_plan* plan, qsft_stream_t stream
       !plan->U || !plan->status)
     return QSFT_ERR_ARG;
   if (plan->prec != QSFT_F32) return QSFT_ERR_ARG;
-  if (plan->gm_mt != 1 && plan->gm_mt != 2 && plan->gm_mt != 4) return QSFT_ERR_ARG;
-  if (plan->gm_npmax < 16 || plan->gm_npmax > 256 || plan->gm_npmax % 16 || plan->gm_mt * plan->gm_npmax > 512)
+  if ((plan->gm_mt != 1 && plan->gm_mt != 2) || (plan->gm_nacc != 1 && plan->gm_nacc != 2)) return QSFT_ERR_ARG;
+  if (plan->gm_npmax < 16 || plan->gm_npmax > 4 * gm::RPC_MAX || plan->gm_npmax % 16 ||
+      gm::tmem_na(plan->gm_mt, plan->gm_nacc, plan->gm_npmax) < 2)
     return QSFT_ERR_ARG;
   if (plan->total_gm_work <= 0) return QSFT_OK;
   cudaStream_t st = (cudaStream_t)stream;

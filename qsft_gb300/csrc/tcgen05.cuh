@@ -38,9 +38,31 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
       : "memory");
   return ok != 0;
 }
+// non-blocking: has the phase of `parity` completed?
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   for (long long i = 0; i < WAIT_LIMIT; ++i)
     if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+// for waits that usually last a long time (a whole work unit): polls spaced by
+// __nanosleep with exponential backoff up to 2 us, so that the waiting warps
+// take no issue slots from the warps doing the work; at most WAIT_LIMIT polls
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity) {
+  unsigned ns = 32;
+  for (long long i = 0; i < WAIT_LIMIT; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    __nanosleep(ns);
+    ns = ns < 2048 ? 2 * ns : 2048;
+  }
   return false;
 }
 __device__ __forceinline__ void tmem_alloc(uint32_t* slot, uint32_t ncols) {
