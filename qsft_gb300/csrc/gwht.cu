@@ -152,7 +152,9 @@ __global__ void __launch_bounds__(512) gwht_pass_kernel(c2<T>* __restrict__ data
 // registers.  The first pass reads global memory and the last one writes it;
 // passes in between go through shared memory, padded by one value every 16 so
 // that every access pattern needs only the minimum of bank wavefronts.  While a row
-// is transformed, the row after next is prefetched into L2.
+// is transformed, the CTA's next row is prefetched into L2 (two rows ahead
+// measured slower: the prefetched lines of 2 x 152 rows start to leave L2
+// before they are read).
 __device__ __forceinline__ int pad16(int e) { return e + (e >> 4); }
 
 template <typename V, int Q, int G>
@@ -269,8 +271,8 @@ __global__ void __launch_bounds__(sizeof(T) == 4 ? 1024 : 512)
   const int npass = (b + DPP - 1) / DPP;
   for (int64_t row = blockIdx.x; row < nrows; row += gridDim.x) {
     c2<T>* x = data + __ldg(row_off + row);
-    if (t == 0 && row + 2 * (int64_t)gridDim.x < nrows) {  // the row after next, into L2
-      const c2<T>* nx = data + __ldg(row_off + row + 2 * (int64_t)gridDim.x);
+    if (t == 0 && row + (int64_t)gridDim.x < nrows) {  // this CTA's next row, into L2
+      const c2<T>* nx = data + __ldg(row_off + row + (int64_t)gridDim.x);
       const uint32_t bytes = (uint32_t)B * (uint32_t)sizeof(c2<T>);
       if (((reinterpret_cast<uintptr_t>(nx) | bytes) & 15) == 0)
         asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(nx), "r"(bytes) : "memory");

@@ -35,12 +35,16 @@ __device__ __forceinline__ double2 box_muller(uint32_t a, uint32_t b, double) {
   sincospi(2.0 * u2, &s, &c);
   return make_double2(r * c, r * s);
 }
+// FP32: the hardware approximations of log and sin/cos (__logf, __sincosf; the
+// angle in [-pi, pi), where sin.approx/cos.approx are accurate to ~2^-20.5):
+// noise needs the distribution, not correctly rounded samples, and the fused
+// GWHT pass is bound by these instructions
 __device__ __forceinline__ float2 box_muller(uint32_t a, uint32_t b, float) {
   const float u1 = ((float)(a >> 8) + 1.0f) * 5.9604645e-08f;  // (0, 1], 24-bit grid
   const float u2 = (float)(b >> 8) * 5.9604645e-08f;           // [0, 1)
-  const float r = sqrtf(-2.0f * logf(u1));
+  const float r = sqrtf(-2.0f * __logf(u1));
   float s, c;
-  sincospif(2.0f * u2, &s, &c);
+  __sincosf(6.2831853f * u2 - 3.1415927f, &s, &c);
   return make_float2(r * c, r * s);
 }
 

@@ -169,6 +169,11 @@ def test_device_noise_statistics(cuda):
     for part in (x.real, x.imag):
         assert abs(part.mean()) < 4 * nu / np.sqrt(part.size)
         assert abs(part.std() / nu - 1) < 0.01
+        z = part / nu
+        assert abs(np.mean(z ** 4) - 3.0) < 0.1                        # kurtosis of the normal
+        assert abs(np.mean(np.abs(z) > 3.0) - 0.0026998) < 6e-4        # two-sided 3-sigma tail mass
+        from scipy import stats
+        assert stats.kstest(z, "norm").statistic < 0.006               # KS distance to N(0, 1)
     assert abs(np.corrcoef(x.real, x.imag)[0, 1]) < 0.01
     bt2 = Batch([sp], precision="fp32")
     bt2.add_noise()
