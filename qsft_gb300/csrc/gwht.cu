@@ -35,6 +35,26 @@ __device__ __forceinline__ void dft_small(V (&x)[Q], const V* __restrict__ tw) {
     x[2] = csub(s02, s13);
     x[1] = cadd(d02, mi);
     x[3] = csub(d02, mi);
+  } else if constexpr (Q == 20) {
+    // 20 = 4 x 5: n = 5 n1 + n2, k = k1 + 4 k2;
+    // X[k1 + 4 k2] = sum_n2 W20^(n2 k1) W5^(n2 k2) sum_n1 x[5 n1 + n2] W4^(n1 k1)
+    V t5[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) t5[j] = tw[4 * j];  // W5^j = W20^(4j)
+    V y[4][5];
+#pragma unroll
+    for (int n2 = 0; n2 < 5; ++n2) {
+      V a[4] = {x[n2], x[5 + n2], x[10 + n2], x[15 + n2]};
+      dft_small<V, 4>(a, tw);
+#pragma unroll
+      for (int k1 = 0; k1 < 4; ++k1) y[k1][n2] = (n2 * k1 == 0) ? a[k1] : cmul(a[k1], tw[n2 * k1]);
+    }
+#pragma unroll
+    for (int k1 = 0; k1 < 4; ++k1) {
+      dft_small<V, 5>(y[k1], t5);
+#pragma unroll
+      for (int k2 = 0; k2 < 5; ++k2) x[k1 + 4 * k2] = y[k1][k2];
+    }
   } else {
     V y[Q];
 #pragma unroll
@@ -49,11 +69,20 @@ __device__ __forceinline__ void dft_small(V (&x)[Q], const V* __restrict__ tw) {
   }
 }
 
+// g / d for 0 <= g < 2^24 through a float reciprocal, corrected to exact
+__device__ __forceinline__ int div_small(int g, int d, float rd) {
+  int h = (int)((float)g * rd);
+  if (h * d > g) --h;
+  else if ((h + 1) * d <= g) ++h;
+  return h;
+}
+
 template <typename T, int Q>
 __device__ __forceinline__ void axis_pass_fixed(c2<T>* tile, int nel, int sm, const c2<T>* tw) {
   const int groups = nel / Q;
+  const float rsm = 1.0f / (float)sm;
   for (int g = threadIdx.x; g < groups; g += blockDim.x) {
-    const int hi = g / sm;
+    const int hi = div_small(g, sm, rsm);
     const int base = hi * sm * Q + (g - hi * sm);
     c2<T> x[Q];
 #pragma unroll
@@ -68,8 +97,9 @@ __device__ __forceinline__ void axis_pass_fixed(c2<T>* tile, int nel, int sm, co
 template <typename T>
 __device__ __forceinline__ void axis_pass_generic(c2<T>* tile, int nel, int sm, int q, const c2<T>* tw) {
   const int groups = nel / q;
+  const float rsm = 1.0f / (float)sm;
   for (int g = threadIdx.x; g < groups; g += blockDim.x) {
-    const int hi = g / sm;
+    const int hi = div_small(g, sm, rsm);
     const int base = hi * sm * q + (g - hi * sm);
     c2<T> x[QSFT_MAX_Q];
     for (int k = 0; k < q; ++k) x[k] = tile[base + k * sm];
@@ -86,10 +116,19 @@ __device__ __forceinline__ void axis_pass_generic(c2<T>* tile, int nel, int sm, 
   }
 }
 
+// device bin noise of one row (noise.cuh); nu = 0: none
+struct RowNoise {
+  uint2 key;
+  int64_t row;  // row index within its job
+  double nu;
+};
+
 template <typename T, int Q>
 __global__ void __launch_bounds__(512) gwht_pass_kernel(c2<T>* __restrict__ data, const int64_t* __restrict__ row_off,
                                                         int q, int naxes, int mid, int inner, int TI, int NO,
-                                                        int tiles_per_row, T divisor) {
+                                                        int tiles_per_row, T inv, int64_t B,
+                                                        const qsft_job* __restrict__ jobs,
+                                                        const int32_t* __restrict__ row_meta) {
   extern __shared__ __align__(16) unsigned char smem[];
   c2<T>* tw = reinterpret_cast<c2<T>*>(smem);
   c2<T>* tile = tw + QSFT_MAX_Q;
@@ -101,6 +140,9 @@ __global__ void __launch_bounds__(512) gwht_pass_kernel(c2<T>* __restrict__ data
   const int o0 = (tr / ti_chunks) * NO;
   const int t0 = (tr - (tr / ti_chunks) * ti_chunks) * TI;
   const int nel = NO * mid * TI;
+  // element e of the tile is (om, t) = (e / TI, e % TI): stepped per thread without division
+  const int t_first = threadIdx.x % TI, om_first = threadIdx.x / TI;
+  const int dt = blockDim.x % TI, dom = blockDim.x / TI;
 
   if (threadIdx.x < q) {
     const double2 w = root_of_unity(threadIdx.x, q);
@@ -110,10 +152,15 @@ __global__ void __launch_bounds__(512) gwht_pass_kernel(c2<T>* __restrict__ data
     const c2<T>* src = x + (int64_t)o0 * mid * inner;
     for (int e = threadIdx.x; e < nel; e += blockDim.x) tile[e] = src[e];
   } else {
+    int t = t_first, om = om_first;  // om = oo*mid + m
     for (int e = threadIdx.x; e < nel; e += blockDim.x) {
-      const int t = e % TI;
-      const int om = e / TI;  // oo*mid + m
       tile[e] = x[((int64_t)o0 * mid + om) * inner + t0 + t];
+      t += dt;
+      om += dom;
+      if (t >= TI) {
+        t -= TI;
+        ++om;
+      }
     }
   }
   __syncthreads();
@@ -125,21 +172,44 @@ __global__ void __launch_bounds__(512) gwht_pass_kernel(c2<T>* __restrict__ data
     else axis_pass_generic<T>(tile, nel, sm, q, tw);
     __syncthreads();
   }
-  const bool scale = divisor != (T)1;
-  if (TI == inner) {
-    c2<T>* dst = x + (int64_t)o0 * mid * inner;
-    for (int e = threadIdx.x; e < nel; e += blockDim.x) {
-      c2<T> v = tile[e];
-      if (scale) { v.x = v.x / divisor; v.y = v.y / divisor; }
-      dst[e] = v;
+  // last pass: scale by 1/q^b and, with jobs, add the row's device bin noise
+  const bool scale = inv != (T)1;
+  RowNoise nz = {make_uint2(0, 0), 0, 0.0};
+  if (jobs) {
+    const qsft_job* jb = jobs + __ldg(row_meta + 2 * row);
+    nz.key = noise_key(jb->noise_seed);
+    nz.row = __ldg(row_meta + 2 * row + 1);
+    nz.nu = jb->noise_nu;
+  }
+  const T tnu = (T)nz.nu;
+  const int64_t half = (B + 1) / 2;
+  auto finish = [&](c2<T> v, int64_t idx) {
+    if (scale) {
+      v.x *= inv;
+      v.y *= inv;
     }
+    if (nz.nu > 0.0) {
+      const c2<T> g = noise_one<T>(nz.key, nz.row, half, idx);
+      v.x += tnu * g.x;
+      v.y += tnu * g.y;
+    }
+    return v;
+  };
+  if (TI == inner) {
+    const int64_t e0 = (int64_t)o0 * mid * inner;
+    c2<T>* dst = x + e0;
+    for (int e = threadIdx.x; e < nel; e += blockDim.x) dst[e] = finish(tile[e], e0 + e);
   } else {
+    int t = t_first, om = om_first;
     for (int e = threadIdx.x; e < nel; e += blockDim.x) {
-      const int t = e % TI;
-      const int om = e / TI;
-      c2<T> v = tile[e];
-      if (scale) { v.x = v.x / divisor; v.y = v.y / divisor; }
-      x[((int64_t)o0 * mid + om) * inner + t0 + t] = v;
+      const int64_t idx = ((int64_t)o0 * mid + om) * inner + t0 + t;
+      x[idx] = finish(tile[e], idx);
+      t += dt;
+      om += dom;
+      if (t >= TI) {
+        t -= TI;
+        ++om;
+      }
     }
   }
 }
@@ -176,13 +246,6 @@ __device__ __forceinline__ void groups_dft(V (&x)[16]) {
     }
   }
 }
-
-// device bin noise of one row (noise.cuh); nu = 0: none
-struct RowNoise {
-  uint2 key;
-  int64_t row;  // row index within its job
-  double nu;
-};
 
 // one pass over digits [d0, d0 + m) with G = q^m; slo = stride of the lowest of them
 template <typename T, int Q, int G>
@@ -347,7 +410,8 @@ __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)
 template <typename T, int Q>
 __global__ void __launch_bounds__(512) gwht_cluster_kernel(c2<T>* __restrict__ data,
                                                            const int64_t* __restrict__ row_off, int q, int b, int k,
-                                                           int CS, T divisor) {
+                                                           int CS, T inv, const qsft_job* __restrict__ jobs,
+                                                           const int32_t* __restrict__ row_meta) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ __align__(16) unsigned char smem[];
@@ -446,13 +510,28 @@ __global__ void __launch_bounds__(512) gwht_cluster_kernel(c2<T>* __restrict__ d
     else axis_pass_generic<T>(part, Bp, stride, q, tw);
     __syncthreads();
   }
-  if (bulk) {
-    for (int e = threadIdx.x; e < Bp; e += blockDim.x) {
-      c2<T> v = part[e];
-      v.x = v.x / divisor;
-      v.y = v.y / divisor;
-      part[e] = v;
+  // scale by 1/q^b and, with jobs, add the row's device bin noise (entry rank*Bp + e)
+  RowNoise nz = {make_uint2(0, 0), 0, 0.0};
+  if (jobs) {
+    const qsft_job* jb = jobs + __ldg(row_meta + 2 * row);
+    nz.key = noise_key(jb->noise_seed);
+    nz.row = __ldg(row_meta + 2 * row + 1);
+    nz.nu = jb->noise_nu;
+  }
+  const T tnu = (T)nz.nu;
+  const int64_t half = ((int64_t)Bp * CS + 1) / 2;
+  auto finish = [&](c2<T> v, int e) {
+    v.x *= inv;
+    v.y *= inv;
+    if (nz.nu > 0.0) {
+      const c2<T> g = noise_one<T>(nz.key, nz.row, half, (int64_t)rank * Bp + e);
+      v.x += tnu * g.x;
+      v.y += tnu * g.y;
     }
+    return v;
+  };
+  if (bulk) {
+    for (int e = threadIdx.x; e < Bp; e += blockDim.x) part[e] = finish(part[e], e);
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
     __syncthreads();
     if (threadIdx.x == 0 && *status) {
@@ -463,12 +542,7 @@ __global__ void __launch_bounds__(512) gwht_cluster_kernel(c2<T>* __restrict__ d
       asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // smem must outlive the copy's reads
     }
   } else {
-    for (int e = threadIdx.x; e < Bp; e += blockDim.x) {
-      c2<T> v = part[e];
-      v.x = v.x / divisor;
-      v.y = v.y / divisor;
-      x[e] = v;
-    }
+    for (int e = threadIdx.x; e < Bp; e += blockDim.x) x[e] = finish(part[e], e);
   }
 }
 
@@ -492,7 +566,7 @@ static int cluster_split(int q, int b, size_t es, int* kout) {
 
 template <typename T, int Q>
 static int launch_cluster(c2<T>* data, const int64_t* row_off, int64_t nrows, int q, int b, int k, int CS,
-                          T divisor, cudaStream_t st) {
+                          T divisor, cudaStream_t st, const qsft_job* jobs, const int32_t* row_meta) {
   int64_t Bp = 1;
   for (int i = k; i < b; ++i) Bp *= q;
   const size_t sm = 16 + (size_t)(Bp + QSFT_MAX_Q) * sizeof(c2<T>);
@@ -511,7 +585,8 @@ static int launch_cluster(c2<T>* data, const int64_t* row_off, int64_t nrows, in
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (cudaLaunchKernelEx(&cfg, kern, data, row_off, q, b, k, CS, divisor) != cudaSuccess) return QSFT_ERR_CUDA;
+  if (cudaLaunchKernelEx(&cfg, kern, data, row_off, q, b, k, CS, (T)1 / divisor, jobs, row_meta) != cudaSuccess)
+    return QSFT_ERR_CUDA;
   QSFT_CUDA_CHECK_LAUNCH();
   return QSFT_OK;
 }
@@ -558,7 +633,7 @@ static int plan_passes(int q, int b, size_t es, size_t budget, Pass* out, int ma
 
 template <typename T, int Q>
 static int launch_pass(c2<T>* data, const int64_t* row_off, int64_t nrows, int q, int b, const Pass& p,
-                       T divisor, cudaStream_t st) {
+                       T divisor, cudaStream_t st, const qsft_job* jobs, const int32_t* row_meta) {
   const int mid = (int)ipow(q, p.a1 - p.a0), inner = (int)ipow(q, b - p.a1), outer = (int)ipow(q, p.a0);
   const int tiles_per_row = (outer / p.NO) * (inner / p.TI);
   const int nel = p.NO * mid * p.TI;
@@ -569,37 +644,9 @@ static int launch_pass(c2<T>* data, const int64_t* row_off, int64_t nrows, int q
   const int64_t grid = nrows * tiles_per_row;
   if (grid > 0x7fffffffLL) return QSFT_ERR_TOO_LARGE;
   kern<<<(unsigned)grid, threads, sm, st>>>(data, row_off, q, p.a1 - p.a0, mid, inner, p.TI, p.NO,
-                                            tiles_per_row, divisor);
+                                            tiles_per_row, (T)1 / divisor, ipow(q, b), jobs, row_meta);
   QSFT_CUDA_CHECK_LAUNCH();
   return QSFT_OK;
-}
-
-// device bin noise of listed rows (shapes the row kernel does not take)
-template <typename T>
-__global__ void noise_rows_kernel(c2<T>* __restrict__ data, const int64_t* __restrict__ row_off, int64_t nrows,
-                                  int64_t B, const qsft_job* __restrict__ jobs, const int32_t* __restrict__ row_meta) {
-  const int64_t half = (B + 1) / 2;
-  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < nrows * half;
-       p += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t i = p / half, e = p - i * half;
-    const qsft_job* jb = jobs + __ldg(row_meta + 2 * i);
-    const double nu = jb->noise_nu;
-    if (!(nu > 0.0)) continue;
-    c2<T> g0, g1;
-    noise_pair<T>(noise_key(jb->noise_seed), __ldg(row_meta + 2 * i + 1), half, e, g0, g1);
-    c2<T>* x = data + __ldg(row_off + i);
-    const T tnu = (T)nu;
-    c2<T> v = x[e];
-    v.x += tnu * g0.x;
-    v.y += tnu * g0.y;
-    x[e] = v;
-    if (e + half < B) {
-      c2<T> w = x[e + half];
-      w.x += tnu * g1.x;
-      w.y += tnu * g1.y;
-      x[e + half] = w;
-    }
-  }
 }
 
 template <typename T>
@@ -619,36 +666,34 @@ static int run_gwht(int q, int b, void* data, const int64_t* row_off, int64_t nr
       return q == 4 ? launch_row<T, 4>(d, row_off, nrows, b, st, jobs, row_meta)
                     : launch_row<T, 2>(d, row_off, nrows, b, st, jobs, row_meta);
   }
-  if (jobs) {  // transform, then the listed rows' noise
-    const int rc = run_gwht<T>(q, b, data, row_off, nrows, st);
-    if (rc != QSFT_OK) return rc;
-    const int64_t B = ipow(q, b), pairs = nrows * ((B + 1) / 2);
-    const int64_t want = (pairs + 255) / 256;
-    noise_rows_kernel<T><<<(unsigned)(want < 152 * 8 ? want : 152 * 8), 256, 0, st>>>(d, row_off, nrows, B, jobs,
-                                                                                        row_meta);
-    QSFT_CUDA_CHECK_LAUNCH();
-    return QSFT_OK;
-  }
+  // other shapes: the noise (jobs non-null) goes into the last pass, one draw per entry
   int k = 0;
   const int CS = cluster_split(q, b, es, &k);
   if (CS > 0) {
     switch (q) {
-      case 2: return launch_cluster<T, 2>(d, row_off, nrows, q, b, k, CS, div, st);
-      case 3: return launch_cluster<T, 3>(d, row_off, nrows, q, b, k, CS, div, st);
-      case 4: return launch_cluster<T, 4>(d, row_off, nrows, q, b, k, CS, div, st);
-      case 5: return launch_cluster<T, 5>(d, row_off, nrows, q, b, k, CS, div, st);
-      default: return launch_cluster<T, 0>(d, row_off, nrows, q, b, k, CS, div, st);
+      case 2: return launch_cluster<T, 2>(d, row_off, nrows, q, b, k, CS, div, st, jobs, row_meta);
+      case 3: return launch_cluster<T, 3>(d, row_off, nrows, q, b, k, CS, div, st, jobs, row_meta);
+      case 4: return launch_cluster<T, 4>(d, row_off, nrows, q, b, k, CS, div, st, jobs, row_meta);
+      case 5: return launch_cluster<T, 5>(d, row_off, nrows, q, b, k, CS, div, st, jobs, row_meta);
+      default: return launch_cluster<T, 0>(d, row_off, nrows, q, b, k, CS, div, st, jobs, row_meta);
     }
   }
   for (int i = 0; i < np; ++i) {
-    const T dv = (i == np - 1) ? div : (T)1;
+    const bool last = i == np - 1;
+    const T dv = last ? div : (T)1;
+    const qsft_job* jl = last ? jobs : nullptr;
+    const int32_t* ml = last ? row_meta : nullptr;
     int rc;
     switch (q) {
-      case 2: rc = launch_pass<T, 2>(d, row_off, nrows, q, b, passes[i], dv, st); break;
-      case 3: rc = launch_pass<T, 3>(d, row_off, nrows, q, b, passes[i], dv, st); break;
-      case 4: rc = launch_pass<T, 4>(d, row_off, nrows, q, b, passes[i], dv, st); break;
-      case 5: rc = launch_pass<T, 5>(d, row_off, nrows, q, b, passes[i], dv, st); break;
-      default: rc = launch_pass<T, 0>(d, row_off, nrows, q, b, passes[i], dv, st); break;
+      case 2: rc = launch_pass<T, 2>(d, row_off, nrows, q, b, passes[i], dv, st, jl, ml); break;
+      case 3: rc = launch_pass<T, 3>(d, row_off, nrows, q, b, passes[i], dv, st, jl, ml); break;
+      case 4: rc = launch_pass<T, 4>(d, row_off, nrows, q, b, passes[i], dv, st, jl, ml); break;
+      case 5: rc = launch_pass<T, 5>(d, row_off, nrows, q, b, passes[i], dv, st, jl, ml); break;
+      case 20:  // 4 x 5 in registers; FP64 keeps the generic DFT (register pressure)
+        rc = sizeof(T) == 4 ? launch_pass<T, 20>(d, row_off, nrows, q, b, passes[i], dv, st, jl, ml)
+                            : launch_pass<T, 0>(d, row_off, nrows, q, b, passes[i], dv, st, jl, ml);
+        break;
+      default: rc = launch_pass<T, 0>(d, row_off, nrows, q, b, passes[i], dv, st, jl, ml); break;
     }
     if (rc != QSFT_OK) return rc;
   }

@@ -59,4 +59,14 @@ __device__ __forceinline__ void noise_pair(uint2 key, int64_t row, int64_t half,
   g1 = box_muller(r.z, r.w, T(0));
 }
 
+// entry e of row `row` alone, for passes whose threads do not hold the pair
+// (e, e + half): the same value noise_pair gives it
+template <typename T>
+__device__ __forceinline__ c2<T> noise_one(uint2 key, int64_t row, int64_t half, int64_t e) {
+  const bool upper = e >= half;
+  const uint64_t ctr = (uint64_t)row * (uint64_t)half + (uint64_t)(upper ? e - half : e);
+  const uint4 r = philox4x32_10(make_uint4((uint32_t)ctr, (uint32_t)(ctr >> 32), 0x9e37u, 0x51f7u), key);
+  return upper ? box_muller(r.z, r.w, T(0)) : box_muller(r.x, r.y, T(0));
+}
+
 }  // namespace qsft

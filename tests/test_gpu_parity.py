@@ -182,13 +182,16 @@ def test_device_noise_statistics(cuda):
 
 @pytest.mark.parametrize("prec", PRECS)
 def test_fused_gwht_noise_equals_separate_passes(cuda, prec):
-    """qsft_gwht_noise (noise added in the transform's last pass, or after it for
-    shapes the row kernel does not take) == qsft_gwht then qsft_add_noise_philox."""
+    """qsft_gwht_noise (noise added in the transform's last pass: pairs of entries
+    in the row kernel, one draw per entry in the tile, cluster and multi-pass
+    kernels) == qsft_gwht then qsft_add_noise_philox."""
     import torch
     from qsft_gb300.engine import Batch, JobSpec
     rng = np.random.RandomState(8)
     specs = []
-    for (q, b, R, P, nu) in [(4, 6, 2, 9, 0.3), (2, 9, 1, 5, 0.2), (3, 5, 2, 4, 0.25), (4, 5, 1, 3, 0.0)]:
+    # row kernel (q in {2, 4}), one-pass tile, cluster (q=5 b=6), two passes (q=5 b=7), q=20 in registers
+    for (q, b, R, P, nu) in [(4, 6, 2, 9, 0.3), (2, 9, 1, 5, 0.2), (3, 5, 2, 4, 0.25), (4, 5, 1, 3, 0.0),
+                             (5, 6, 1, 7, 0.2), (5, 7, 1, 8, 0.15), (20, 3, 1, 4, 0.1), (20, 4, 1, 5, 0.05)]:
         C = 2
         U = torch.from_numpy(rng.randn(C, R * P, q ** b) + 1j * rng.randn(C, R * P, q ** b))
         n = P - 1                                   # identity source: P - 1 >= n
