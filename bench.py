@@ -249,33 +249,25 @@ def run_serving(args, dev):
 # ------------------------------------------------------------------ GPU
 def run_ours(args):
     import torch
-    import torch.distributed as dist
     from qsft_gb300 import _lib
+    from qsft_gb300 import replicas as RP
     from qsft_gb300.engine import Batch
     from qsft_gb300.serve import TransformStream, transform_batch
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    # N GPUs = N independent replicas (no data-path collective): each rank runs
+    # its own batches; barriers and the max of the per-rank times for timing
+    rank, world, local = RP.init_from_env()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    if world > 1:
-        dist.init_process_group("nccl", device_id=dev)
     lib = _lib.load()
     J = args.batch
     reqs = make_requests(J, args.seed + 1000 * rank)
 
     def barrier():
-        if world > 1:
-            dist.barrier()
+        RP.barrier()
         torch.cuda.synchronize()
 
-    def max_over_ranks(x):
-        if world == 1:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    max_over_ranks = RP.max_over_ranks
 
     # ---- device-resident throughput (value) + per-kernel timing
     batch = Batch([r.spec() for r in reqs], precision=args.precision, device=dev)
@@ -393,8 +385,7 @@ def run_ours(args):
     serving = run_serving(args, dev) if args.serve_requests > 0 else None
 
     if rank != 0:
-        if world > 1:
-            dist.destroy_process_group()
+        RP.shutdown()
         return
     # ---- roofline of the dominant kernel (coset evaluation) and of the GWHT
     w = WORKLOAD
@@ -461,8 +452,7 @@ def run_ours(args):
         v, cores, sample = cpu_baseline(sample_rows=2, seed=args.seed)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
     print(json.dumps(line), flush=True)
-    if world > 1:
-        dist.destroy_process_group()
+    RP.shutdown()
 
 
 if __name__ == "__main__":
