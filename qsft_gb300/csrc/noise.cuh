@@ -32,7 +32,7 @@ __device__ __forceinline__ double2 box_muller(uint32_t a, uint32_t b, double) {
   const double u2 = (double)b * 2.3283064365386963e-10;          // [0, 1)
   const double r = sqrt(-2.0 * log(u1));
   double s, c;
-  sincospi(2.0 * u2, &s, &c);
+  sincospi(2.0 * u2 - 1.0, &s, &c);  // the FP32 draw's angle 2 pi u2 - pi: one noise realisation
   return make_double2(r * c, r * s);
 }
 // FP32: the hardware approximations of log and sin/cos (__logf, __sincosf; the
@@ -40,9 +40,10 @@ __device__ __forceinline__ double2 box_muller(uint32_t a, uint32_t b, double) {
 // noise needs the distribution, not correctly rounded samples, and the fused
 // GWHT pass is bound by these instructions
 __device__ __forceinline__ float2 box_muller(uint32_t a, uint32_t b, float) {
-  const float u1 = ((float)(a >> 8) + 1.0f) * 5.9604645e-08f;  // (0, 1], 24-bit grid
-  const float u2 = (float)(b >> 8) * 5.9604645e-08f;           // [0, 1)
-  const float r = sqrtf(-2.0f * __logf(u1));
+  // the FP64 draw's uniforms rounded to FP32 (small u1 exact: the tail matches too)
+  const float u1 = ((float)a + 1.0f) * 2.3283064e-10f;  // (0, 1]
+  const float u2 = (float)b * 2.3283064e-10f;           // [0, 1]
+  const float r = sqrtf(fmaxf(-2.0f * __logf(u1), 0.0f));  // __logf's absolute error near 1: no NaN
   float s, c;
   __sincosf(6.2831853f * u2 - 3.1415927f, &s, &c);
   return make_float2(r * c, r * s);

@@ -180,6 +180,26 @@ def test_device_noise_statistics(cuda):
     assert np.array_equal(bt2.job_U(0).cpu().numpy().ravel(), x), "same seed must give the same noise"
 
 
+def test_device_noise_is_one_realisation_in_fp32_and_fp64(cuda):
+    """The FP32 and FP64 plans draw the same device noise (the FP32 Box-Muller
+    uses hardware approximations of log and sin/cos on the same angle), so the
+    batched FP32 path and the plain FP64 path see the same noisy bins."""
+    import torch
+    from qsft_gb300.engine import Batch, JobSpec
+    q, n, b, C, R, P = 5, 6, 5, 2, 2, 7
+    out = {}
+    for prec, dt in (("fp32", torch.complex64), ("fp64", torch.complex128)):
+        U = torch.zeros(C, R * P, q ** b, dtype=dt, device=cuda)
+        sp = JobSpec(q, n, b, np.zeros((C, n, b)), np.zeros((C, R * P, n)), R, P, U=U, noise_nu=1.0, noise_seed=99)
+        bt = Batch([sp], precision=prec)
+        bt.add_noise()
+        out[prec] = bt.job_U(0).cpu().numpy().astype(np.complex128).ravel()
+    # FP32 rounding of the uniforms and the approximations: ~1e-6 of a unit normal
+    d = np.abs(out["fp32"] - out["fp64"])
+    assert np.quantile(d, 0.999) < 2e-5 and np.max(d) < 1e-3
+    assert np.mean(d) < 2e-6
+
+
 @pytest.mark.parametrize("prec", PRECS)
 def test_fused_gwht_noise_equals_separate_passes(cuda, prec):
     """qsft_gwht_noise (noise added in the transform's last pass: pairs of entries
