@@ -102,6 +102,24 @@ class JobSpec:
         if src == "coded" and rs is None:
             raise ValueError("coded source needs a ReedSolomon description")
 
+    @classmethod
+    def trusted(cls, q, n, b, M, D, R, P, chan, src, cutoff, K, A, rs, max_iter, noise_nu, noise_seed):
+        """A JobSpec from arrays that already passed __init__'s conversions and
+        checks (int64 M (C, n, b), D (C, R*P, n), K (S, n); complex128 A): the
+        per-submit path of a request whose arrays were validated once."""
+        sp = cls.__new__(cls)
+        sp.q, sp.n, sp.b, sp.R, sp.P = q, n, b, R, P
+        sp.M, sp.D, sp.C = M, D, M.shape[0]
+        sp.chan, sp.src, sp.rs, sp.cutoff = chan, src, rs, float(cutoff)
+        sp.K, sp.A = K, A
+        sp.S = 0 if K is None else K.shape[0]
+        sp.U = None
+        sp.max_iter = int(max_iter)
+        sp.noise_nu = float(noise_nu)
+        sp.noise_seed = int(noise_seed) & ((1 << 64) - 1)
+        sp.B = q ** b
+        return sp
+
 
 def workspace_bytes(specs, precision="fp32"):
     """Device bytes a :class:`Batch` of `specs` allocates (its workspace, inputs

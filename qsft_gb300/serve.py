@@ -38,28 +38,29 @@ class TransformRequest:
         self.noise_seed = int(noise_seed)
         self.cutoff = cutoff if cutoff is not None else 1e-9 + 1.5 * self.noise_sd ** 2 / self.q ** self.b
         self.max_iter = max_iter
+        self._arrays = None   # (M, D, K, A, rs) stacked and checked at the first spec()
 
     @property
     def S(self):
         return self.locq.shape[1]
 
-    def footprint_bytes(self, precision="fp32"):
-        """Device bytes this request occupies while in flight (bins + peeling scratch)."""
-        C, R, P, B = len(self.Ms), len(self.Ds[0]), self.Ds[0][0].shape[0], self.q ** self.b
-        es = 8 if precision == "fp32" else 16
-        bins = C * B
-        slots = 1 << int(np.ceil(np.log2(max(64, 2 * bins))))
-        kst = ((self.n + 15) // 16) * 16
-        return C * R * P * B * es + bins * (kst + 16) + slots * 24 + (bins + 64) * (kst + 20)
-
     def spec(self):
-        C = len(self.Ms)
+        """The request as a JobSpec.  Its stacked, converted and checked arrays are
+        made once (a request's support, coefficients, M and D do not change);
+        each call builds a fresh JobSpec from them with the current scalars."""
         R, P = len(self.Ds[0]), self.Ds[0][0].shape[0]
-        D = np.stack([np.vstack(Dg) for Dg in self.Ds])
-        rs = ReedSolomon(self.n, self.t, self.q) if self.src == "coded" else None
-        return JobSpec(self.q, self.n, self.b, np.stack(self.Ms), D, R, P, chan=self.chan, src=self.src,
-                       cutoff=self.cutoff, K=self.locq.T, A=self.strengths, rs=rs, max_iter=self.max_iter,
-                       noise_nu=self.noise_sd / np.sqrt(2 * self.q ** self.b), noise_seed=self.noise_seed)
+        nu = self.noise_sd / np.sqrt(2 * self.q ** self.b)
+        if self._arrays is None:
+            D = np.stack([np.vstack(Dg) for Dg in self.Ds])
+            rs = ReedSolomon(self.n, self.t, self.q) if self.src == "coded" else None
+            sp = JobSpec(self.q, self.n, self.b, np.stack(self.Ms), D, R, P, chan=self.chan, src=self.src,
+                         cutoff=self.cutoff, K=self.locq.T, A=self.strengths, rs=rs, max_iter=self.max_iter,
+                         noise_nu=nu, noise_seed=self.noise_seed)
+            self._arrays = (sp.M, sp.D, sp.K, sp.A, rs)
+            return sp
+        M, D, K, A, rs = self._arrays
+        return JobSpec.trusted(self.q, self.n, self.b, M, D, R, P, self.chan, self.src, self.cutoff, K, A, rs,
+                               self.max_iter, nu, self.noise_seed)
 
 
 def random_request(q, n, b, S, C=3, R=2, snr_db=None, chan="nso", src="identity", t=None, a_min=1.0, a_max=10.0,
