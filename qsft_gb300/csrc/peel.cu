@@ -233,7 +233,8 @@ __device__ __forceinline__ V group_sum_g(V v, unsigned mask, int g) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(DEC_THREADS, 4) decode_kernel(qsft_plan plan) {
+// FP32: 6 blocks per SM (80 registers, no spill; measured 2% faster than 4)
+__global__ void __launch_bounds__(DEC_THREADS, sizeof(T) == 4 ? 6 : 4) decode_kernel(qsft_plan plan) {
   if (__ldcg(plan.done_count) >= plan.njobs) return;  // every job has left the loop
   __shared__ float2 s_w[33 * 32];                            // roots, FP32
   __shared__ c2<T> s_col[DEC_BINS][DEC_STAGE_RP];
