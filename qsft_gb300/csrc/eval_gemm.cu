@@ -453,9 +453,7 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
         }
       }
       const ModQ mq = make_modq(x.q);
-      // the store of slot `pend` is still in flight while the next chunk is
-      // computed; its afull is signalled once the store has completed
-      int pend = -1;
+      // each chunk is computed before its slot is free (the wait overlaps the work)
       for (int kc = 0; kc < x.nK; ++kc) {
         const int s0 = kc * (KC / KPS);
         uint32_t av[32];  // the row's 64 FP16 entries of this chunk, K order
@@ -491,13 +489,6 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
             av[4 * i + 3] = h1.y;
           }
         }
-        if (pend >= 0) {
-          tmem_st_wait();
-          tc_fence_before();
-          __syncwarp();
-          if (lane == 0) mbar_arrive(&afull[pend]);
-          pend = -1;
-        }
         if (g >= (uint32_t)NA) {  // slot reuse: the MMAs of chunk g - NA have completed
           int go = 1;
           if (lane == 0) go = !*abort_flag && mbar_wait(&cons[ce.slot], ce.phase);
@@ -508,16 +499,14 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
           }
           ce.next();
         }
+        // store and signal at once: the MMA warp waits for this chunk, not for the next one's compute
         tmem_st32(a_lane + fa.slot * (uint32_t)(MT * A_COLS), av);
-        pend = (int)fa.slot;
-        fa.next();
-        ++g;
-      }
-      if (pend >= 0) {
         tmem_st_wait();
         tc_fence_before();
         __syncwarp();
-        if (lane == 0) mbar_arrive(&afull[pend]);
+        if (lane == 0) mbar_arrive(&afull[fa.slot]);
+        fa.next();
+        ++g;
       }
     }
   } else if (warp < mma_warp) {
