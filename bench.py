@@ -155,7 +155,7 @@ def coef_nmse(keys, vals, req):
 
 # DRAM bytes per launch from one ncu capture of this workload (dram__bytes_read.sum +
 # dram__bytes_write.sum; profiles/eval_gemm_q4n20b7_batch16.md, profiles/gwht_row_q4n20b7_batch16.md)
-NCU_TRAFFIC = {"eval": (35.08e6 + 203.15e6) + (12.81e6 + 12.40e6), "gwht": 267.84e6 + 216.44e6, "batch": 16}
+NCU_TRAFFIC = {"eval": (35.07e6 + 203.33e6) + (12.94e6 + 12.53e6), "gwht": 267.81e6 + 216.15e6, "batch": 16}
 
 
 def run_reference(args):
