@@ -517,7 +517,9 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
       const long long u = next_unit(uqr);
       if (u < 0) break;
       int ok = 1;
-      if (lane == 0) ok = !*abort_flag && mbar_wait_sleep(&accf[ac.slot], ac.phase);
+      // one accumulator buffer: the MMA warp waits for this drain, so notice the
+      // unit's end soon (128 ns cap); two: the drain overlaps MMAs, sleep longer
+      if (lane == 0) ok = !*abort_flag && mbar_wait_sleep(&accf[ac.slot], ac.phase, nacc == 1 ? 128u : 2048u);
       ok = __shfl_sync(~0u, ok, 0);
       if (!ok) {
         if (lane == 0) *abort_flag = 1;

@@ -54,14 +54,15 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
   return false;
 }
 // for waits that usually last a long time (a whole work unit): polls spaced by
-// __nanosleep with exponential backoff up to 2 us, so that the waiting warps
-// take no issue slots from the warps doing the work; at most WAIT_LIMIT polls
-__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity) {
+// __nanosleep with exponential backoff up to max_ns, so that the waiting warps
+// take few issue slots from the warps doing the work (a shorter cap notices the
+// phase sooner); at most WAIT_LIMIT polls
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity, unsigned max_ns = 2048) {
   unsigned ns = 32;
   for (long long i = 0; i < WAIT_LIMIT; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
     __nanosleep(ns);
-    ns = ns < 2048 ? 2 * ns : 2048;
+    ns = ns < max_ns ? 2 * ns : max_ns;
   }
   return false;
 }
