@@ -71,7 +71,7 @@ class Clocks:
              "clocks_event_reasons.sw_power_cap")
         try:
             self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu_index}", f"--query-gpu={q}", "--format=csv,noheader",
-                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+                                       "-lms", "50"], stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.p = None
 
@@ -304,7 +304,16 @@ def run_ours(args):
     for _ in range(max(args.warmup, 3)):
         batch.run()
     barrier()
+    # clocks: sampled every 50 ms from an untimed ~0.4 s run of the same step
+    # just before the timed steps until their end (the K timed steps alone are
+    # shorter than one sample)
     clk = Clocks(local)
+    t_soak = time.perf_counter()
+    while time.perf_counter() - t_soak < 0.4:
+        for _ in range(20):
+            batch.run()
+        torch.cuda.synchronize()
+    barrier()
     t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0e.record(stream)
     for _ in range(args.steps):
@@ -330,22 +339,24 @@ def run_ours(args):
     # pipelines the steps (host packing / parsing of one batch overlaps the
     # GPU's work on the next); every step still packs and uploads its inputs
     # and reads back its results inside the timed region
-    ts = TransformStream(precision=args.precision)
+    # a ring of three workspaces, two batches in flight: the host's packing and
+    # parsing of one batch hides behind the GPU's work on the next two
+    from collections import deque
+    ts = TransformStream(precision=args.precision, depth=3)
     for _ in range(max(args.warmup, 3)):
-        t_a = ts.submit(reqs)
-        t_b = ts.submit(reqs)
-        ts.result(t_a)
-        ts.result(t_b)
+        tks = [ts.submit(reqs) for _ in range(3)]
+        for tk in tks:
+            ts.result(tk)
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    prev = None
+    inflight = deque()
     for i in range(args.steps):
-        tk = ts.submit(reqs)
-        if prev is not None:
-            ts.result(prev)
-        prev = tk
-    ts.result(prev)
+        inflight.append(ts.submit(reqs))
+        if len(inflight) > 2:
+            ts.result(inflight.popleft())
+    while inflight:
+        ts.result(inflight.popleft())
     torch.cuda.synchronize()
     e2e_s = max_over_ranks(time.perf_counter() - t0)
     e2e = J * args.steps * world / e2e_s
