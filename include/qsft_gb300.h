@@ -260,12 +260,13 @@ int qsft_gwht(int prec, int q, int b, void* data, const int64_t* row_off, int64_
               qsft_stream_t stream);
 
 /*
- * qsft_gwht over rows of plan->U (row_off as for qsft_gwht) followed by the
- * device bin noise of qsft_add_noise_philox for those rows, fused into the
- * transform's last pass where the shape allows (q in {2, 4}): the bins are
- * read and written once.  row_meta[2i], row_meta[2i+1] = the job of row i and
- * the row's index within that job (c*R*P + r*P + p).  Jobs with noise_nu = 0
- * get the plain transform.
+ * qsft_gwht over rows of plan->U (row_off as for qsft_gwht) with the device bin
+ * noise of qsft_add_noise_philox for those rows added in the transform's last
+ * pass, for every shape (the row kernel draws once per entry pair, the other
+ * kernels once per entry; the values are those of the separate noise pass):
+ * no extra read and write of the bins.  row_meta[2i], row_meta[2i+1] = the job
+ * of row i and the row's index within that job (c*R*P + r*P + p).  Jobs with
+ * noise_nu = 0 get the plain transform.
  */
 int qsft_gwht_noise(const qsft_plan* plan, int q, int b, const int64_t* row_off, const int32_t* row_meta,
                     int64_t nrows, qsft_stream_t stream);

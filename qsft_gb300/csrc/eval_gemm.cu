@@ -29,24 +29,26 @@
 // than K keeps K at 2 (or 4) entries per support vector, so each MMA reads
 // fewer operand bytes from shared memory per multiply-add: that read rate,
 // not the multiplier array, bounds a single-CTA MMA with N <= 256.  Delay rows
-// go in chunks of up to 64 (N <= 256).  An operand kernel writes B (and the
+// go in equal chunks of at most 56 (N <= 224, so two accumulator buffers of a
+// 128-row tile still fit tensor memory).  An operand kernel writes B (and the
 // packed j_s digits) into a workspace in the exact shared-memory image of each
 // 64-entry K chunk (128-byte-swizzled K-major rows), so the GEMM kernel streams
-// it with one bulk copy per stage.  The GEMM kernel generates A in shared memory
-// from the row's digits (two dp4a per support vector for b <= 8) and issues
-// tcgen05.mma kind::f16 (M = 128, N, K = 16) into tensor memory.
+// it with one bulk copy per chunk.  The GEMM kernel generates A in tensor
+// memory from the row's digits (two dp4a per support vector for b <= 8) and
+// issues tcgen05.mma kind::f16 (M = 128, N, K = 16) into tensor memory.
 //
 // Work unit: MT tiles of 128 rows of one (job, group, chunk of delay rows).
-// The GEMM kernel is persistent (one CTA per SM over a cost-balanced range of
-// units) with four roles: producer warps (one thread per row) write A chunks
+// The GEMM kernel is persistent (one CTA per SM; units taken from a global
+// counter) with four roles: producer warps (one thread per row) write A chunks
 // into a tensor-memory ring, one warp issues the MMAs, one warp streams the B
-// chunks into a shared-memory ring with bulk copies, and epilogue warps read the
-// accumulators back (tcgen05.ld) and store U.  Both rings and the one or two
-// accumulator buffers are guarded by mbarriers: afull (producers wrote A) /
-// aempty (the MMAs that read it completed), bfull (bulk copy landed) / bempty,
-// accf (a unit's MMAs completed) / acce (its accumulators were read).  Every
-// wait is bounded; on a timeout the CTA sets plan.status, drains its copies
-// and MMAs (bounded) and frees its tensor memory.
+// chunks into a shared-memory ring with bulk copies (and hands out the units),
+// and epilogue warps read the accumulators back (tcgen05.ld) and store U.
+// mbarriers: afull (producers wrote A) / bfull (bulk copy landed), one "chunk
+// consumed" barrier per B slot that frees both rings (one commit per chunk),
+// accf (a unit's MMAs completed) / acce (its accumulators were read), and the
+// unit queue's full / empty.  Every wait is bounded; on a timeout the CTA sets
+// plan.status, drains its copies and MMAs (bounded) and frees its tensor
+// memory.
 #include "common.cuh"
 #include "tcgen05.cuh"
 
