@@ -126,8 +126,10 @@ constexpr int PREP_MAXN = QSFT_MAX_N;
 constexpr int PREP_MAXRP = 128;
 template <int KPS, int NW>
 __global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
-  __shared__ int8_t sK[PREP_S * PREP_MAXN];
-  __shared__ int8_t sD[PREP_MAXRP * PREP_MAXN];
+  // k_s and delay rows as int8 digits, rows padded with zeros to whole 32-bit
+  // words (stride np4) so that <d, k> is a run of dp4a
+  __shared__ __align__(16) int8_t sK[PREP_S * PREP_MAXN];
+  __shared__ __align__(16) int8_t sD[PREP_MAXRP * PREP_MAXN];
   __shared__ float2 sW[QSFT_MAX_Q];
   __shared__ float red[8];
   const int nj = plan.njobs;
@@ -150,8 +152,15 @@ __global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
   unsigned char* rc = region + REGION_HDR + (int64_t)c * g.region_c;
   const int tid = threadIdx.x;
 
-  for (int i = tid; i < s_live * n; i += blockDim.x) sK[i] = K[i];
-  for (int i = tid; i < RP * n; i += blockDim.x) sD[i] = D[i];
+  const int np4 = (n + 3) & ~3, nw4 = np4 >> 2;
+  for (int i = tid; i < s_live * np4; i += blockDim.x) {
+    const int r = i / np4, k = i - r * np4;
+    sK[i] = k < n ? K[r * n + k] : (int8_t)0;
+  }
+  for (int i = tid; i < RP * np4; i += blockDim.x) {
+    const int r = i / np4, k = i - r * np4;
+    sD[i] = k < n ? D[r * n + k] : (int8_t)0;
+  }
   if (tid < q) {
     const double* r = plan.roots + ((int64_t)q * 32 + tid) * 2;
     sW[tid] = make_float2((float)r[0], (float)r[1]);
@@ -185,7 +194,7 @@ __global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
         const int t = wi * 4 + k;
         if (t >= b) break;
         int acc = 0;
-        for (int i = 0; i < n; ++i) acc += (int)M[i * b + t] * (int)sK[sl * n + i];
+        for (int i = 0; i < n; ++i) acc += (int)M[i * b + t] * (int)sK[sl * np4 + i];
         uint32_t v = (uint32_t)(acc % q);
         if (KPS == 2 && q == 2) v *= 2;
         word |= v << (8 * k);
@@ -211,8 +220,10 @@ __global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
     const int h = rp / g.RPC, nb = 4 * (rp - h * g.RPC);
     uint32_t rh = 0, rl = 0, ih = 0, il = 0;
     if (sl < s_live) {
+      const int* dw = reinterpret_cast<const int*>(sD + rp * np4);
+      const int* kw = reinterpret_cast<const int*>(sK + sl * np4);
       int acc = 0;
-      for (int i = 0; i < n; ++i) acc += (int)sD[rp * n + i] * (int)sK[sl * n + i];
+      for (int w = 0; w < nw4; ++w) acc = __dp4a(dw[w], kw[w], acc);
       const float2 wr = sW[acc % q];
       const float2 a = A[s];
       const float cr = (a.x * wr.x - a.y * wr.y) * sc;
