@@ -52,6 +52,57 @@ def test_gwht_sizes_vs_oracle(cuda, prec, q, b):
 
 
 @pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("q,b", [(4, 11), (2, 22)])
+def test_gwht_largest_rows_vs_oracle(cuda, prec, q, b):
+    """Rows of q^b = 2^22 values, the largest the C ABI takes (passes through global memory)."""
+    import torch
+    from qsft_gb300.engine import gwht_device
+    rs = np.random.RandomState(b)
+    x = rs.randn(1, q ** b) + 1j * rs.randn(1, q ** b)
+    t = torch.from_numpy(x).to(cuda).to(torch.complex128 if prec == "fp64" else torch.complex64)
+    got = gwht_device(t, q, b).cpu().numpy()
+    want = O.gwht(x[0], q, b)[None]
+    assert rel_err(got, want) < REL[prec] * 3
+
+
+def _small_qsft(prec, a_min, a_max, S, seed):
+    import qsft_gb300 as Q
+    q, n, b, C = 4, 10, 4, 3
+    qa = dict(query_method="complex", num_subsample=C, delays_method_source="identity",
+              subsampling_method="qsft", delays_method_channel="identity", num_repeat=1, b=b)
+    np.random.seed(seed)
+    sig = Q.get_random_subsampled_signal(n=n, q=q, sparsity=S, a_min=a_min, a_max=a_max, noise_sd=0.0,
+                                         query_args=dict(qa), precision=prec)
+    res = Q.QSFT(num_subsample=C, num_repeat=1, b=b, reconstruct_method_source="identity",
+                 reconstruct_method_channel="identity").transform(sig, report=True)
+    np.random.seed(seed)
+    osig = O.OracleSignal(n, q, S, a_min, a_max, 0.0, dict(qa))
+    want = O.OracleQSFT(num_subsample=C, num_repeat=1, b=b, reconstruct_method_source="identity",
+                        reconstruct_method_channel="identity").transform(osig)
+    return res, {tuple(int(x) for x in k): v for k, v in want.items()}
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_zero_signal_gives_empty_result(cuda, prec):
+    """Every coefficient zero: no bin passes the energy test, the loop stops after
+    its first iteration and the result is empty (the report as the reference's:
+    no locations, Hamming weights 0)."""
+    res, want = _small_qsft(prec, 0.0, 0.0, 20, 3)
+    assert want == {}
+    assert res["gwht"] == {} and res["locations"] == []
+    assert res["avg_hamming_weight"] == 0 and res["max_hamming_weight"] == 0
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_single_coefficient(cuda, prec):
+    res, want = _small_qsft(prec, 1.0, 10.0, 1, 4)
+    got = res["gwht"]
+    assert set(got) == set(want) and len(want) == 1
+    k = next(iter(want))
+    assert abs(got[k] - want[k]) <= REL[prec] * abs(want[k])
+
+
+@pytest.mark.parametrize("prec", PRECS)
 @pytest.mark.parametrize("q,n,S", [(4, 20, 1000), (20, 10, 37), (5, 100, 50), (3, 7, 1), (2, 128, 130)])
 def test_eval_points_vs_oracle(cuda, prec, q, n, S):
     from qsft_gb300.engine import eval_points_device
