@@ -235,25 +235,57 @@ class Batch:
         self.gwht_meta_host = {k: np.concatenate(v).ravel() for k, v in meta.items()}
         self.max_iter = max(sp.max_iter for sp in specs)
 
+    def _index_block(self):
+        """The small index arrays the kernels read (job prefixes, GF tables, GWHT
+        row offsets and row metadata, the GEMM work index), packed into one int64
+        host array so that they reach the device in one copy: (array,
+        {name: (word offset, length, dtype)}, GEMM work index or None).  Every
+        segment starts 16 bytes after a multiple of 16."""
+        J = self.njobs
+        segs = [("eval_prefix", np.asarray(self.eval_prefix_host, dtype=np.int64), torch.int64),
+                ("bin_prefix", np.array([self.jobs_host[j].off_bin for j in range(J)] + [self.total_bins],
+                                        dtype=np.int64), torch.int64),
+                ("tc_prefix", np.asarray(self.tc_prefix_host, dtype=np.int64), torch.int64),
+                ("gf", np.ascontiguousarray(self.gf_host, dtype=np.int32), torch.int32)]
+        for k, v in self.gwht_rows_host.items():
+            segs.append((("rows", k), np.ascontiguousarray(v, dtype=np.int64), torch.int64))
+        for k, v in self.gwht_meta_host.items():
+            segs.append((("meta", k), np.ascontiguousarray(v, dtype=np.int32), torch.int32))
+        gm_index = None
+        if self.prec == QSFT_F32:
+            index = (ctypes.c_int64 * (3 * J + 2))()
+            if self.lib.qsft_gemm_layout(self.jobs_host, J, ctypes.byref(QsftPlan()), index) == 0:
+                gm_index = np.frombuffer(index, dtype=np.int64).copy()
+                segs.append(("gm_index", gm_index, torch.int64))
+        place, words = {}, 0
+        for name, arr, dt in segs:
+            place[name] = (words, arr.size, dt)
+            words += max(2, (arr.nbytes + 15) // 16 * 2)
+        block = np.zeros(words, dtype=np.int64)
+        raw = block.view(np.uint8)
+        for name, arr, _ in segs:
+            off = place[name][0] * 8
+            raw[off:off + arr.nbytes] = arr.view(np.uint8)
+        return block, place, gm_index
+
     def planned_bytes(self):
         """Bytes ``_allocate`` takes for this layout, each buffer rounded up to the
         caching allocator's 512-byte blocks."""
         J, es = self.njobs, (8 if self.prec == QSFT_F32 else 16)
         bins, slots, balls, ks = self.total_bins, self.total_slots, self.total_balls, self.kstride
         cs = ctypes.sizeof(QsftCtrl) // 8
+        block, _, _ = self._index_block()
         sizes = [max(self.n_i8, 1), max(self.n_a, 1) * es, max(self.n_u, 1) * es, ctypes.sizeof(QsftJob) * J,
-                 (J + 1) * 8, (J + 1) * 8, (J + 1) * 8, self.gf_host.size * 4,     # prefixes, GF tables
+                 block.nbytes,                                                      # packed index arrays
                  bins * 16, bins * ks, slots * 8, balls * 8, balls * 4,             # rho, kbuf, ball table, best, uniq
                  balls * ks, balls * 16, balls * 4,                                 # ball k, sum, count
                  bins, bins * 4, 2 * bins * 4, bins * 4,                            # status, stamp, dirty, cand
                  balls * ks, balls * 16, balls * 4, (2 + 2 * J + cs * J) * 8, 4]    # outputs, metadata, done
-        sizes += [8 * len(v) for v in self.gwht_rows_host.values()]
-        sizes += [4 * len(v) for v in self.gwht_meta_host.values()]
         if self.prec == QSFT_F32:
             p = QsftPlan()
             index = (ctypes.c_int64 * (3 * J + 2))()
             if self.lib.qsft_gemm_layout(self.jobs_host, J, ctypes.byref(p), index) == 0:
-                sizes += [max(int(p.gm_ws_bytes), 256), (3 * J + 2) * 8]
+                sizes.append(max(int(p.gm_ws_bytes), 256))
         return int(sum((s + 511) // 512 * 512 for s in sizes))
 
     def device_bytes(self):
@@ -276,14 +308,23 @@ class Batch:
         self.A = z(self.n_a, self.cdt)
         self.U = torch.empty(max(self.n_u, 1), dtype=self.cdt, device=dev)
         self.jobs_dev = z(ctypes.sizeof(QsftJob) * J, torch.uint8)
-        up = lambda a, d: torch.from_numpy(np.ascontiguousarray(a)).to(dev, dtype=d)  # noqa: E731
-        self.eval_prefix = up(np.array(self.eval_prefix_host, dtype=np.int64), torch.int64)
-        self.bin_prefix = up(np.array([self.jobs_host[j].off_bin for j in range(J)] + [self.total_bins],
-                                      dtype=np.int64), torch.int64)
-        self.tc_prefix = up(np.array(self.tc_prefix_host, dtype=np.int64), torch.int64)
-        self.gf = up(self.gf_host, torch.int32)
-        self.gwht_groups = {k: up(v, torch.int64) for k, v in self.gwht_rows_host.items()}
-        self.gwht_meta = {k: up(v, torch.int32) for k, v in self.gwht_meta_host.items()}
+        # the small index arrays: one pinned staging buffer, one copy on the current
+        # stream, typed views into one device buffer
+        block, place, gm_index = self._index_block()
+        self._index_host = torch.from_numpy(block).pin_memory()
+        self.index_dev = torch.empty(block.size, dtype=torch.int64, device=dev)
+        self.index_dev.copy_(self._index_host, non_blocking=True)
+
+        def view(name):
+            w, n, dt = place[name]
+            if dt == torch.int64:
+                return self.index_dev[w:w + n]
+            return self.index_dev[w:w + (n + 1) // 2].view(torch.int32)[:n]
+
+        self.eval_prefix, self.bin_prefix = view("eval_prefix"), view("bin_prefix")
+        self.tc_prefix, self.gf = view("tc_prefix"), view("gf")
+        self.gwht_groups = {k: view(("rows", k)) for k in self.gwht_rows_host}
+        self.gwht_meta = {k: view(("meta", k)) for k in self.gwht_meta_host}
         self.roots = roots_table(dev)
         self.rho = z(self.total_bins * 2, torch.float64)
         self.kbuf = z(self.total_bins * self.kstride, torch.uint8)
@@ -336,12 +377,13 @@ class Batch:
         p.tc_entry_bytes = self.tc_entry_bytes
         p.status = ptr(self.status)
         # coset-factored GEMM evaluation (FP32): operand workspace and work index
+        # (the layout call fills the plan's gm_* fields; its index is in the block)
         index = (ctypes.c_int64 * (3 * J + 2))()
-        self.gm_ok = (self.prec == QSFT_F32 and
+        self.gm_ok = (gm_index is not None and
                       self.lib.qsft_gemm_layout(self.jobs_host, J, ctypes.byref(p), index) == 0)
         if self.gm_ok:
             self.gm_ws = torch.empty(max(int(p.gm_ws_bytes), 256), dtype=torch.uint8, device=dev)
-            self.gm_index = up(np.frombuffer(index, dtype=np.int64).copy(), torch.int64)
+            self.gm_index = view("gm_index")
             p.gm_ws, p.gm_index = ptr(self.gm_ws), ptr(self.gm_index)
         self.plan = p
 
