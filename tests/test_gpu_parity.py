@@ -334,6 +334,7 @@ def _random_spec(rng, q, n, b, S, C, R, chan="nso"):
     [(3, 40, 5, 700, 2, 1)],                       # K=64
     [(5, 100, 3, 50, 3, 1)],                       # K=128
     [(20, 10, 3, 1500, 2, 1)],                     # support split over several chunks
+    [(3, 12, 9, 200, 2, 1)],                       # runtime q with b > 8: four words of digits
     [(4, 12, 5, 60, 3, 2), (3, 9, 4, 20, 3, 1), (20, 6, 2, 30, 3, 3), (2, 16, 8, 40, 3, 2)],  # mixed batch
 ])
 @pytest.mark.parametrize("method", ["gemm", "tc"])
