@@ -14,7 +14,8 @@ the whole budget can never run and is failed at once.
 The loop is host logic only; the device work sits behind an executor:
 
     footprint(request) -> bytes      launch(requests) -> handle
-    poll() -> [(handle, results)]    wait(until)      now()
+    poll() -> [(handle, results or the exception that ended the batch)]
+    wait(until)                      now()
 
 ``GpuExecutor`` runs each batch as one :class:`~qsft_gb300.engine.Batch`
 (evaluation, GWHT with device noise, peeling, collection; one launch per
@@ -22,7 +23,8 @@ phase) and reads its results back asynchronously.  Tests drive the same loop
 with a simulated executor and clock.
 
 Failures are handled on the host.  ``launch`` raising fails that batch's
-requests and frees its memory.  A batch that has not finished after
+requests and frees its memory, and so does a batch whose results could not be
+read (a device status or table overflow reported by ``poll``).  A batch that has not finished after
 ``batch_timeout`` seconds has its requests failed; its memory stays reserved
 until the executor reports it finished, because its kernels may still be
 writing there.
@@ -102,6 +104,9 @@ class Server:
                 idx, nbytes, _, timed_out = inflight.pop(h)
                 used -= nbytes
                 if timed_out:
+                    continue
+                if isinstance(results, Exception):
+                    fail(idx, f"batch failed: {type(results).__name__}: {results}")
                     continue
                 t_done = ex.now() - t0
                 for i, res in zip(idx, results):
@@ -194,9 +199,10 @@ def poisson_arrivals(n, rate, rng=None):
 # ---------------------------------------------------------------- the GPU
 class GpuExecutor:
     """Batches on CUDA streams of their own: each ``launch`` packs its requests
-    into a fresh :class:`~qsft_gb300.engine.Batch` (allocated on that stream),
-    issues the whole step and an asynchronous result read-back there, and
-    returns at once."""
+    into a fresh :class:`~qsft_gb300.engine.Batch` (allocated and uploaded on
+    the current stream), issues the whole step and an asynchronous result
+    read-back on a stream of its own, and returns at once.  ``poll`` hands back a
+    batch's results, or the exception raised while reading them."""
 
     def __init__(self, precision="fp32", max_inflight=4, device=None):
         import torch
@@ -245,8 +251,11 @@ class GpuExecutor:
         out = []
         for h in [h for h, (b, _) in self.inflight.items() if b.fetched_event.query()]:
             b, si = self.inflight.pop(h)
-            res = [TransformResult(k, v, c, int(ctrl.iter)) for k, v, c, ctrl in b.results_fetched()]
             self.free_streams.append(si)
+            try:
+                res = [TransformResult(k, v, c, int(ctrl.iter)) for k, v, c, ctrl in b.results_fetched()]
+            except Exception as e:  # noqa: BLE001 -- a device error fails this batch's requests only
+                res = e
             out.append((h, res))
         return out
 

@@ -16,12 +16,14 @@ class SimExecutor:
     """A device that runs the batches in flight one after another (in launch
     order), a batch taking the sum of its requests' work; `fail_launch` makes
     ``launch`` raise for batches containing those requests, `hang` makes those
-    batches finish only after `hang_s` seconds."""
+    batches finish only after `hang_s` seconds, `fail_result` makes ``poll``
+    report an exception instead of those batches' results."""
 
-    def __init__(self, launch_cost=1e-4, fail_launch=(), hang=(), hang_s=100.0):
+    def __init__(self, launch_cost=1e-4, fail_launch=(), hang=(), hang_s=100.0, fail_result=()):
         self.t = 0.0
         self.launch_cost = launch_cost
         self.fail_launch, self.hang, self.hang_s = set(fail_launch), set(hang), hang_s
+        self.fail_result = set(fail_result)
         self.device_free = 0.0
         self.inflight = {}
         self.launched = []
@@ -57,7 +59,10 @@ class SimExecutor:
         for h in [h for h, (_, tf) in self.inflight.items() if tf <= self.t]:
             reqs, _ = self.inflight.pop(h)
             self.bytes -= sum(r.nbytes for r in reqs)
-            out.append((h, [("done", r.i) for r in reqs]))
+            if any(r.i in self.fail_result for r in reqs):
+                out.append((h, RuntimeError("injected device status")))
+            else:
+                out.append((h, [("done", r.i) for r in reqs]))
         return out
 
     def wait(self, until):
@@ -140,6 +145,16 @@ def test_launch_failure_fails_only_that_batch():
     assert rep.errors[5] is not None and "injected" in rep.errors[5]
     assert rep.completed() == 11
     assert ex.bytes == 0
+
+
+def test_batch_whose_results_fail_fails_only_its_requests():
+    reqs = [Req(i, 10, 1e-3) for i in range(10)]
+    arr = np.arange(10) * 0.01
+    ex = SimExecutor(fail_result={3})
+    rep = Server(ex, budget_bytes=1000, max_jobs=1).run(reqs, arr)
+    assert rep.errors[3] is not None and "injected device status" in rep.errors[3]
+    assert np.isnan(rep.latency[3]) and rep.results[3] is None
+    assert rep.completed() == 9 and ex.bytes == 0
 
 
 def test_stuck_batch_times_out_but_keeps_its_memory():
