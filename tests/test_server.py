@@ -211,3 +211,35 @@ def test_footprint_matches_layout_on_host():
     assert all(x > 0 for x in one)
     # a packed batch needs about the sum of its members (wider key rows when n differs)
     assert 0.5 * sum(one) <= both <= 2.0 * sum(one)
+
+
+def test_index_block_segments_decode_back():
+    """The small index arrays of a mixed batch, packed for one copy to the device:
+    every segment is 16-byte aligned and holds exactly its host array."""
+    import torch
+    from qsft_gb300 import _lib
+    from qsft_gb300.engine import Batch, precision_code
+    np.random.seed(5)
+    specs = [random_mix_request().spec() for _ in range(12)]
+    for prec in ("fp32", "fp64"):
+        b = Batch.__new__(Batch)
+        b.lib, b.prec = _lib.load(), precision_code(prec)
+        b._build_layout(specs)
+        block, place, gm = b._index_block()
+        assert (gm is not None) == (prec == "fp32")
+        raw = block.view(np.uint8)
+        want = {"eval_prefix": np.asarray(b.eval_prefix_host, np.int64),
+                "tc_prefix": np.asarray(b.tc_prefix_host, np.int64),
+                "gf": np.asarray(b.gf_host, np.int32)}
+        want.update({("rows", k): v.astype(np.int64) for k, v in b.gwht_rows_host.items()})
+        want.update({("meta", k): v.astype(np.int32) for k, v in b.gwht_meta_host.items()})
+        if gm is not None:
+            want["gm_index"] = gm
+        for name, arr in want.items():
+            w, n, dt = place[name]
+            assert (w * 8) % 16 == 0 and n == arr.size
+            got = raw[w * 8:w * 8 + arr.nbytes].view(np.int64 if dt == torch.int64 else np.int32)
+            assert np.array_equal(got, arr), name
+        spans = sorted((w, w + max(2, (n * (8 if dt == torch.int64 else 4) + 15) // 16 * 2))
+                       for w, n, dt in place.values())
+        assert all(a[1] <= b_[0] for a, b_ in zip(spans, spans[1:]))   # no overlap
