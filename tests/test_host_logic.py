@@ -69,3 +69,41 @@ def test_codecs():
     big = [3 ** 60 - 1, 12345678901234567890123]
     assert np.array_equal(U.dec_to_qary_vec(np.array(big, dtype=object), 3, 60), O.dec_to_qary_vec(big, 3, 60))
     assert np.array_equal(U.qary_ints(3, 4), O.qary_ints(3, 4))
+
+
+def test_jobspec_rejects_what_the_kernels_cannot_take():
+    import pytest
+    from qsft_gb300.engine import JobSpec
+    M, D = np.zeros((1, 4, 2)), np.zeros((1, 5, 4))
+    with pytest.raises(ValueError):
+        JobSpec(1, 4, 2, M, D, 1, 5)                        # q < 2
+    with pytest.raises(ValueError):
+        JobSpec(33, 4, 2, M, D, 1, 5)                       # q above 32
+    with pytest.raises(ValueError):
+        JobSpec(2, 4, 23, np.zeros((1, 4, 23)), D, 1, 5)    # q^b above 2^22
+    with pytest.raises(ValueError):
+        JobSpec(4, 4, 2, M - 1, D, 1, 5)                    # negative digit
+    with pytest.raises(ValueError):
+        JobSpec(4, 4, 2, M, D, 1, 5, src="coded")           # coded source without its code
+
+
+def test_request_spec_is_built_once_and_stays_equal():
+    """spec() stacks and checks a request's arrays at the first call; later calls
+    build a JobSpec from them with the current scalars, equal to a fresh one."""
+    from qsft_gb300.engine import JobSpec
+    from qsft_gb300.serve import random_request
+    np.random.seed(2)
+    r = random_request(4, 12, 5, 40, C=3, R=2, snr_db=10.0)
+    first, again = r.spec(), r.spec()
+    fresh = JobSpec(r.q, r.n, r.b, np.stack(r.Ms), np.stack([np.vstack(d) for d in r.Ds]), 2, r.n + 1,
+                    chan="nso", cutoff=r.cutoff, K=r.locq.T, A=r.strengths,
+                    noise_nu=r.noise_sd / np.sqrt(2 * r.q ** r.b), noise_seed=r.noise_seed)
+    for sp in (first, again):
+        for k in ("q", "n", "b", "C", "R", "P", "S", "B", "chan", "src", "cutoff", "max_iter", "noise_nu",
+                  "noise_seed"):
+            assert getattr(sp, k) == getattr(fresh, k), k
+        for k in ("M", "D", "K", "A"):
+            assert np.array_equal(getattr(sp, k), getattr(fresh, k)), k
+    assert again.M is first.M          # the stacked arrays are shared, not rebuilt
+    r.noise_seed = 12345               # scalars are read at every call
+    assert r.spec().noise_seed == 12345
