@@ -343,24 +343,30 @@ int qsft_rs_decode(int q, int s, int t, int n, const int32_t* gf_tables, const u
 /*
  * No counterpart in the reference: the peeling loop of qsft_peel_init +
  * qsft_peel_run + qsft_collect for ONE job, for callers that cannot allocate
- * device memory -- code being captured into a CUDA graph (cudaMalloc and
- * cudaFree cannot be captured), serving threads that must not stall on
- * cudaMalloc's device-wide synchronisation, plugin hosts that own every
- * buffer.  All scratch (hash tables, result store, lists, roots table, control
- * record) lives in a statically sized device array inside the library (about
- * 2.4 MB, held by every GPU that loads the library until the process exits),
- * so the call allocates nothing.  `job` is a host record (offsets off_M/off_D
- * into i8, off_U into U; qsft_workspace_layout's fields are filled in by the
- * call); U holds the job's bins and is peeled in place.  Results as
- * qsft_collect, rows of QSFT_NOALLOC_KSTRIDE bytes; max_out must be at least
- * C*q^b + 64.  Limits: C*q^b <= QSFT_NOALLOC_MAX_BINS, n <= 32, else
- * QSFT_ERR_TOO_LARGE.  Every call shares the one array: calls that overlap on
- * the GPU race; serialise them.  The first call on a device looks up the
- * array's address with that device current; make it before any stream capture.
+ * device memory: serving threads that must not stall on cudaMalloc's
+ * device-wide synchronisation while other streams are busy, and host
+ * applications that own every buffer (a fixed memory budget or a pool of
+ * their own) and hand a library only its inputs and outputs.  All scratch
+ * (hash tables, result store, lists, roots table, control record) lives in a
+ * statically sized device array inside the library (about 2.4 MB, held by
+ * every GPU that loads the library until the process exits), so the call
+ * allocates nothing.  `job` is a host record (offsets off_M/off_D into i8,
+ * off_U into U; qsft_workspace_layout's fields are filled in by the call); U
+ * holds the job's bins and is peeled in place.  Results as qsft_collect, rows
+ * of QSFT_NOALLOC_KSTRIDE bytes; max_out must be at least C*q^b + 64.
+ * out_ctrl (device memory, required) receives the job's control record when
+ * the loop has ended: out_ctrl->err != 0 (QSFT_ERR_OVERFLOW) means a device
+ * table filled up and the results are incomplete; iter, n_balls and
+ * num_peeling are those of the workspace path.  Limits: C*q^b <=
+ * QSFT_NOALLOC_MAX_BINS, n <= 32, else QSFT_ERR_TOO_LARGE.  Every call shares
+ * the one array and its contents stay from the last call: calls that overlap
+ * on the GPU race; serialise them.  The first call on a device looks up the
+ * array's address with that device current; make it before any stream
+ * capture.
  */
 int qsft_peel_noalloc(int prec, const qsft_job* job, const int8_t* i8, void* U, const int32_t* gf_tables,
                       uint8_t* out_k, double* out_val, int32_t* out_cnt, int64_t* out_total, int32_t max_out,
-                      qsft_stream_t stream);
+                      qsft_ctrl* out_ctrl, qsft_stream_t stream);
 
 /*
  * Scratch sizes for a batch: given the jobs' (q, n, b, C, B) on the host,

@@ -123,7 +123,7 @@ def load():
         "qsft_peel_run": ([plan_p, i32, vp], i32),
         "qsft_collect": ([plan_p, vp, vp, vp, vp, vp, vp], i32),
         "qsft_rs_decode": ([i32, i32, i32, i32, vp, vp, i64, vp, vp], i32),
-        "qsft_peel_noalloc": ([i32, ctypes.POINTER(QsftJob), vp, vp, vp, vp, vp, vp, vp, i32, vp], i32),
+        "qsft_peel_noalloc": ([i32, ctypes.POINTER(QsftJob), vp, vp, vp, vp, vp, vp, vp, i32, vp, vp], i32),
         "qsft_workspace_layout": ([ctypes.POINTER(QsftJob), i32, ctypes.POINTER(i64), ctypes.POINTER(i64),
                                    ctypes.POINTER(i64), ctypes.POINTER(ctypes.c_int32)], i32),
     }

@@ -118,6 +118,7 @@ extern "C" const char* qsft_status_string(int status) {
     case QSFT_ERR_CUDA: return "CUDA error";
     case QSFT_ERR_TOO_LARGE: return "shape exceeds a compiled limit";
     case QSFT_ERR_OVERFLOW: return "device table overflow";
+    case QSFT_ERR_TIMEOUT: return "a bounded device wait gave up";
     default: return "unknown status";
   }
 }

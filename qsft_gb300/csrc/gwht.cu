@@ -407,11 +407,19 @@ static int launch_row(c2<T>* data, const int64_t* row_off, int64_t nrows, int b,
 // taking an equal share of the groups; axes k..b-1 are local to each part.
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
+// A part is moved by the TMA engine (one bulk copy and a bounded mbarrier wait)
+// only when the call has a status word to report a timed-out wait to
+// (status_word non-null) and the part is 16-byte aligned; otherwise by plain
+// loads.  After a timed-out wait no CTA of the cluster touches the row: each
+// CTA reads every peer's flag through DSMEM after the first cluster barrier,
+// so the whole cluster skips the exchange and the stores alike, and the first
+// CTA records QSFT_ERR_TIMEOUT in the status word.
 template <typename T, int Q>
 __global__ void __launch_bounds__(512) gwht_cluster_kernel(c2<T>* __restrict__ data,
                                                            const int64_t* __restrict__ row_off, int q, int b, int k,
                                                            int CS, T inv, const qsft_job* __restrict__ jobs,
-                                                           const int32_t* __restrict__ row_meta) {
+                                                           const int32_t* __restrict__ row_meta,
+                                                           int* __restrict__ status_word) {
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   extern __shared__ __align__(16) unsigned char smem[];
@@ -426,7 +434,7 @@ __global__ void __launch_bounds__(512) gwht_cluster_kernel(c2<T>* __restrict__ d
   c2<T>* __restrict__ x = data + __ldg(row_off + row) + (int64_t)rank * Bp;
   const uint32_t bytes = (uint32_t)Bp * (uint32_t)sizeof(c2<T>);
   // the TMA engine moves the part when source, destination and size are 16-byte aligned
-  const bool bulk = ((reinterpret_cast<uintptr_t>(x) | bytes) & 15) == 0;
+  const bool bulk = status_word != nullptr && ((reinterpret_cast<uintptr_t>(x) | bytes) & 15) == 0;
   if (threadIdx.x == 0) {
     *status = 1;
     if (bulk) {
@@ -467,6 +475,14 @@ __global__ void __launch_bounds__(512) gwht_cluster_kernel(c2<T>* __restrict__ d
     for (int e = threadIdx.x; e < Bp; e += blockDim.x) part[e] = x[e];
   }
   cluster.sync();
+  // every part landed? (the same answer in every CTA of the cluster)
+  bool all_ok = true;
+  for (int r = 0; r < CS; ++r) all_ok &= *cluster.map_shared_rank(status, r) != 0;
+  if (!all_ok) {
+    if (rank == 0 && threadIdx.x == 0 && status_word) atomicExch(status_word, (int)QSFT_ERR_TIMEOUT);
+    cluster.sync();  // peers have read this CTA's flag before it exits
+    return;
+  }
   // ---- axes spanning the cluster
   const int ngroups = (CS / q) * Bp;  // per axis
   const int per = ngroups / CS;
@@ -566,7 +582,8 @@ static int cluster_split(int q, int b, size_t es, int* kout) {
 
 template <typename T, int Q>
 static int launch_cluster(c2<T>* data, const int64_t* row_off, int64_t nrows, int q, int b, int k, int CS,
-                          T divisor, cudaStream_t st, const qsft_job* jobs, const int32_t* row_meta) {
+                          T divisor, cudaStream_t st, const qsft_job* jobs, const int32_t* row_meta,
+                          int* status_word) {
   int64_t Bp = 1;
   for (int i = k; i < b; ++i) Bp *= q;
   const size_t sm = 16 + (size_t)(Bp + QSFT_MAX_Q) * sizeof(c2<T>);
@@ -585,7 +602,8 @@ static int launch_cluster(c2<T>* data, const int64_t* row_off, int64_t nrows, in
   attr[0].val.clusterDim.z = 1;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  if (cudaLaunchKernelEx(&cfg, kern, data, row_off, q, b, k, CS, (T)1 / divisor, jobs, row_meta) != cudaSuccess)
+  if (cudaLaunchKernelEx(&cfg, kern, data, row_off, q, b, k, CS, (T)1 / divisor, jobs, row_meta, status_word) !=
+      cudaSuccess)
     return QSFT_ERR_CUDA;
   QSFT_CUDA_CHECK_LAUNCH();
   return QSFT_OK;
@@ -651,7 +669,7 @@ static int launch_pass(c2<T>* data, const int64_t* row_off, int64_t nrows, int q
 
 template <typename T>
 static int run_gwht(int q, int b, void* data, const int64_t* row_off, int64_t nrows, cudaStream_t st,
-                    const qsft_job* jobs = nullptr, const int32_t* row_meta = nullptr) {
+                    const qsft_job* jobs = nullptr, const int32_t* row_meta = nullptr, int* status_word = nullptr) {
   const size_t es = sizeof(c2<T>);
   const size_t budget = 200 * 1024 - QSFT_MAX_Q * es;
   Pass passes[24];
@@ -671,11 +689,11 @@ static int run_gwht(int q, int b, void* data, const int64_t* row_off, int64_t nr
   const int CS = cluster_split(q, b, es, &k);
   if (CS > 0) {
     switch (q) {
-      case 2: return launch_cluster<T, 2>(d, row_off, nrows, q, b, k, CS, div, st, jobs, row_meta);
-      case 3: return launch_cluster<T, 3>(d, row_off, nrows, q, b, k, CS, div, st, jobs, row_meta);
-      case 4: return launch_cluster<T, 4>(d, row_off, nrows, q, b, k, CS, div, st, jobs, row_meta);
-      case 5: return launch_cluster<T, 5>(d, row_off, nrows, q, b, k, CS, div, st, jobs, row_meta);
-      default: return launch_cluster<T, 0>(d, row_off, nrows, q, b, k, CS, div, st, jobs, row_meta);
+      case 2: return launch_cluster<T, 2>(d, row_off, nrows, q, b, k, CS, div, st, jobs, row_meta, status_word);
+      case 3: return launch_cluster<T, 3>(d, row_off, nrows, q, b, k, CS, div, st, jobs, row_meta, status_word);
+      case 4: return launch_cluster<T, 4>(d, row_off, nrows, q, b, k, CS, div, st, jobs, row_meta, status_word);
+      case 5: return launch_cluster<T, 5>(d, row_off, nrows, q, b, k, CS, div, st, jobs, row_meta, status_word);
+      default: return launch_cluster<T, 0>(d, row_off, nrows, q, b, k, CS, div, st, jobs, row_meta, status_word);
     }
   }
   for (int i = 0; i < np; ++i) {
@@ -711,8 +729,10 @@ extern "C" int qsft_gwht_noise(const qsft_plan* plan, int q, int b, const int64_
   if (nrows == 0) return QSFT_OK;
   if (!row_off || !row_meta) return QSFT_ERR_ARG;
   cudaStream_t st = (cudaStream_t)stream;
-  if (plan->prec == QSFT_F32) return run_gwht<float>(q, b, plan->U, row_off, nrows, st, plan->jobs, row_meta);
-  if (plan->prec == QSFT_F64) return run_gwht<double>(q, b, plan->U, row_off, nrows, st, plan->jobs, row_meta);
+  if (plan->prec == QSFT_F32)
+    return run_gwht<float>(q, b, plan->U, row_off, nrows, st, plan->jobs, row_meta, plan->status);
+  if (plan->prec == QSFT_F64)
+    return run_gwht<double>(q, b, plan->U, row_off, nrows, st, plan->jobs, row_meta, plan->status);
   return QSFT_ERR_ARG;
 }
 

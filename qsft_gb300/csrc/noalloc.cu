@@ -1,20 +1,23 @@
 // Peeling of one transform without any device allocation.
 //
 // Some callers cannot allocate device memory when they run the transform:
-// code that is being captured into a CUDA graph (cudaMalloc/cudaFree are not
-// capturable), serving threads that must not hit cudaMalloc's implicit device
-// synchronisation in the middle of other streams' work, and plugin hosts that
-// own every buffer and hand the library only its inputs and outputs.  For
-// them qsft_peel_noalloc runs QSFT.transform's peeling loop for one job with
-// all of its scratch in g_scratch below, a statically sized device array that
-// every GPU loading this library holds until the process exits.
+// serving threads that must not hit cudaMalloc's implicit device-wide
+// synchronisation while other streams are busy, and host applications that
+// own every buffer (a fixed memory budget or a pool of their own) and hand a
+// library only its inputs and outputs.  For them qsft_peel_noalloc runs
+// QSFT.transform's peeling loop for one job with all of its scratch in
+// g_scratch below, a statically sized device array that every GPU loading
+// this library holds until the process exits.
 //
 // Limits: C*B <= QSFT_NOALLOC_MAX_BINS bins and n <= QSFT_NOALLOC_KSTRIDE.
-// Every call shares the array: calls that overlap on the GPU (different
-// streams, threads or processes' contexts on one device) race and corrupt each
-// other's results; serialise them.  The first call on a device takes the
-// array's device address (cudaGetSymbolAddress) with that device current, so
-// make that first call before any stream capture.
+// Every call shares the array, and it keeps the last call's contents:
+// qsft_peel_init clears what must start at zero, and calls that overlap on
+// the GPU (different streams, threads or processes' contexts on one device)
+// race and corrupt each other's results; serialise them.  The first call on a
+// device takes the array's device address (cudaGetSymbolAddress) with that
+// device current, so make that first call before any stream capture.  The
+// job's control record is copied to the caller's out_ctrl at the end, so a
+// table overflow (ctrl.err) reaches the caller like on the workspace path.
 #include <mutex>
 
 #include "common.cuh"
@@ -95,8 +98,9 @@ using namespace qsft::noalloc;
 
 extern "C" int qsft_peel_noalloc(int prec, const qsft_job* job_in, const int8_t* i8, void* U,
                                  const int32_t* gf_tables, uint8_t* out_k, double* out_val, int32_t* out_cnt,
-                                 int64_t* out_total, int32_t max_out, qsft_stream_t stream) {
-  if (!job_in || !i8 || !U || !out_k || !out_val || !out_cnt || !out_total) return QSFT_ERR_ARG;
+                                 int64_t* out_total, int32_t max_out, qsft_ctrl* out_ctrl,
+                                 qsft_stream_t stream) {
+  if (!job_in || !i8 || !U || !out_k || !out_val || !out_cnt || !out_total || !out_ctrl) return QSFT_ERR_ARG;
   if (prec != QSFT_F32 && prec != QSFT_F64) return QSFT_ERR_ARG;
   qsft_job job = *job_in;
   int64_t bins = 0, slots = 0, balls = 0;
@@ -152,5 +156,11 @@ extern "C" int qsft_peel_noalloc(int prec, const qsft_job* job_in, const int8_t*
   if (rc != QSFT_OK) return rc;
   rc = qsft_peel_run(&p, job.max_iter, stream);
   if (rc != QSFT_OK) return rc;
-  return qsft_collect(&p, out_k, out_val, out_cnt, reinterpret_cast<int64_t*>(base + OFF_INDEX), out_total, stream);
+  rc = qsft_collect(&p, out_k, out_val, out_cnt, reinterpret_cast<int64_t*>(base + OFF_INDEX), out_total, stream);
+  if (rc != QSFT_OK) return rc;
+  // the control record (err, iter, n_balls, num_peeling) to the caller: a
+  // device-to-device copy on the stream, no allocation
+  if (cudaMemcpyAsync(out_ctrl, base + OFF_CTRL, sizeof(qsft_ctrl), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+    return QSFT_ERR_CUDA;
+  return QSFT_OK;
 }

@@ -1,9 +1,9 @@
 """Generate the golden fixtures in this folder by running the reference q-SFT.
 
 This script is the only committed code that executes the reference
-(basics-lab/qsft, mounted read-only at /root/reference in the build
-container).  It is run once, by hand, in a container that has the reference
-checkout; the fixtures it writes (``*.npz``) are committed and travel with the
+(basics-lab/qsft).  It is run once, by hand, on a machine that has a checkout
+of the reference, given by ``--ref PATH`` or the ``QSFT_REFERENCE`` environment
+variable; the fixtures it writes (``*.npz``) are committed and travel with the
 repository, the reference itself does not.
 
 The reference needs packages this image lacks.  The shims below replace them
@@ -17,7 +17,7 @@ with stand-ins that are never reached on the q-SFT path:
 * ``multiprocess.Pool`` (synthetic_signal.py:6) becomes a thread pool with
   ``imap`` -- evaluation order and results are unchanged.
 
-Usage:  python tests/golden/make_golden.py [case ...]
+Usage:  python tests/golden/make_golden.py --ref PATH [case ...]
 """
 import copy
 import os
@@ -28,7 +28,7 @@ from multiprocessing.pool import ThreadPool
 
 import numpy as np
 
-REF = "/root/reference"
+REF = os.environ.get("QSFT_REFERENCE")   # the reference checkout (or --ref PATH)
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -69,6 +69,8 @@ def _install_shims():
     for m in ["galois._codes", "galois._codes._reed_solomon"]:
         sys.modules[m] = types.ModuleType(m)
     sys.modules["galois._codes._reed_solomon"].decode_jit = None
+    if not REF or not os.path.isdir(os.path.join(REF, "qsft")):
+        raise SystemExit("give the reference checkout with --ref PATH or QSFT_REFERENCE=PATH")
     sys.path.insert(0, REF)
 
 
@@ -234,8 +236,13 @@ def test_qary_pins():
 
 
 if __name__ == "__main__":
+    args = sys.argv[1:]
+    if "--ref" in args:
+        i = args.index("--ref")
+        REF = args[i + 1]
+        del args[i:i + 2]
     _install_shims()
-    names = sys.argv[1:] or list(CASES) + ["gwht", "test_qary"]
+    names = args or list(CASES) + ["gwht", "test_qary"]
     for nm in names:
         if nm == "gwht":
             gwht_pins()
