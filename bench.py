@@ -11,13 +11,17 @@ GWHT, noise, peeling (all 15 loop iterations issued; finished jobs no-op) and
 result collection.  Every batch holds > 129 MB of bins, so successive steps
 stream from HBM rather than L2.
 
-  value  transforms/s with inputs resident on the device (CUDA events)
+  value  transforms/s with inputs resident on the device (CUDA events); the
+         steps alternate between two captured workspaces on two streams, so
+         two batches are in flight as in e2e (the serial replay of one
+         workspace on one stream is reported beside it)
   e2e    transforms/s through qsft_gb300.serve.transform_batch with host
          inputs, host->device copies of those inputs and the device->host read
          of every result inside the timed region (wall clock + sync)
 
 --impl reference times the reference's CPU algorithm (the numpy restatement in
-oracle/) on the host cores on a bounded sample of the same workload.
+oracle/) on the host cores: every step is one whole transform of the same
+workload, timed (oracle/cpu_baseline.py).
 """
 import argparse
 import json
@@ -35,7 +39,6 @@ sys.path.insert(0, ROOT)
 WORKLOAD = dict(q=4, n=20, b=7, S=1000, C=3, R=2, snr_db=10.0, chan="nso", src="identity")
 METRIC = "sparse transforms/s (q=4,n=20,b=7,C=3,NSO R=2,S=1000,10 dB), FP32-batched vs FP64-plain"
 UNIT = "transforms/s"
-SAMPLE_ROWS = 16   # coset rows the CPU baseline evaluates (of 126), scaled to all: ~10 s of CPU work
 
 
 def parse():
@@ -101,47 +104,33 @@ class Clocks:
 
 
 # ------------------------------------------------------------------ CPU baseline
-def cpu_baseline(sample_rows=SAMPLE_ROWS, seed=0):
-    """The oracle (numpy restatement of the reference) on this host's cores:
-    evaluation of `sample_rows` of the 126 coset rows (threaded over all
-    cores, scaled to 126), plus the full GWHT of all rows and the full peeling
-    loop.  Returns (transforms/s, cores, sample description)."""
-    import oracle as O
-    w = WORKLOAD
-    q, n, b, S, C, R = w["q"], w["n"], w["b"], w["S"], w["C"], w["R"]
-    cores = os.cpu_count() or 1
-    np.random.seed(seed)
-    qa = dict(query_method="complex", num_subsample=C, b=b, delays_method_source="identity",
-              delays_method_channel="nso", num_repeat=R)
-    nsd = O.noise_sd_for_snr(S, w["snr_db"])
-    sig = O.OracleSignal(n, q, S, 1, 10, nsd, qa, skip_sampling=True)
-    P = n + 1
-    rows = C * R * P
-    # 1. evaluation sample
-    t0 = time.perf_counter()
-    for r in range(sample_rows):
-        c, rr = divmod(r, R * P)
-        X = O.coset_points(sig.Ms[c], sig.Ds[c][rr // P][rr % P], q).T
-        O.eval_points(X, sig.locq, sig.strengths, q, threads=cores)
-    t_eval = (time.perf_counter() - t0) * rows / sample_rows
-    # 2. GWHT of every row (bins from the closed form stand in for the samples' transform input)
-    Dst = [np.vstack(d) for d in sig.Ds]
-    U = O.closed_form_bins(sig.Ms, Dst, sig.locq, sig.strengths, q)
-    t0 = time.perf_counter()
-    for c in range(C):
-        for r in range(R * P):
-            O.gwht(U[c, r], q, b)
-    t_gwht = time.perf_counter() - t0
-    # 3. noise + peeling on the full bins
-    sig.Us = [[U[c, r * P:(r + 1) * P] for r in range(R)] for c in range(C)]
-    t0 = time.perf_counter()
-    O.OracleQSFT(num_subsample=C, num_repeat=R, b=b, reconstruct_method_source="identity",
-                 reconstruct_method_channel="nso").transform(sig)
-    t_peel = time.perf_counter() - t0
-    total = t_eval + t_gwht + t_peel
-    sample = (f"eval of {sample_rows}/{rows} coset rows (x{rows / sample_rows:.2f} scaled, {cores} threads) + "
-              f"full GWHT ({t_gwht:.2f}s) + full noise+peeling ({t_peel:.2f}s); est. {total:.1f}s/transform")
-    return 1.0 / total, cores, sample
+# The reference itself (Python, numpy/scipy, multiprocess pool), measured by
+# running it on 8 x86 cores at this workload and seed 0: 107.4 s per transform.
+REFERENCE_MEASURED_S = 107.4
+
+
+def cpu_transforms(steps, warmup, seed=0):
+    """Time `steps` whole transforms of the workload with the oracle (the numpy
+    restatement of the reference) on all host cores, in a child process whose
+    BLAS runs one thread per worker (oracle/cpu_baseline.py).  Nothing is
+    sampled or scaled.  Returns the child's JSON record (per-step seconds,
+    threads used)."""
+    env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1", MKL_NUM_THREADS="1")
+    r = subprocess.run([sys.executable, "-m", "oracle.cpu_baseline", "--steps", str(steps), "--warmup", str(warmup),
+                        "--seed", str(seed)], cwd=ROOT, env=env, capture_output=True, text=True, check=True)
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def cpu_baseline_record(rec):
+    steps = len(rec["step_s"])
+    value = steps / sum(rec["step_s"])
+    sample = (f"{steps} whole transforms (signal, all {WORKLOAD['C'] * WORKLOAD['R'] * (WORKLOAD['n'] + 1)} coset "
+              f"rows evaluated with the reference's exp(2 pi i XK/q)@a, GWHT, noise, peeling; nothing scaled), "
+              f"{rec['threads']} threads x 1 BLAS thread on {rec['machine']}: "
+              f"{np.mean(rec['step_s']):.2f} s per transform; the reference itself measured "
+              f"{REFERENCE_MEASURED_S} s per transform on 8 x86 cores")
+    return {"value": value, "unit": UNIT, "cores": rec["threads"], "kind": "port", "sample": sample,
+            "step_s": rec["step_s"], "reference_measured_s_per_transform": REFERENCE_MEASURED_S}
 
 
 def coef_nmse(keys, vals, req):
@@ -154,29 +143,92 @@ def coef_nmse(keys, vals, req):
     return float(err / sum(abs(a) ** 2 for a in true.values()))
 
 
+def _key_dict(keys, vals):
+    return {tuple(int(x) for x in k): complex(v) for k, v in zip(keys, vals)}
+
+
+def pin_vs_oracle(reqs, dev, precision="fp32", seed=123, max_entries=1 << 22):
+    """Each request through the GPU path and through the oracle on the same bin
+    noise, drawn on the host (numpy, one RandomState per request): the GPU
+    evaluates the cosets and transforms them (its bins are compared with the
+    oracle's closed-form bins, sum_{s: M^T k_s = j} a_s omega^<d, k_s>, the
+    identity that sampling + GWHT reproduces), adds the noise and peels; the
+    oracle peels (qsft/qsft.py:151-255 restated in numpy, FP64) the closed-form
+    bins plus the same noise.  Requests with more than `max_entries` bin
+    entries (C*R*P*q^b) are skipped.  Returns one record per request compared."""
+    import torch
+    import oracle as O
+    from qsft_gb300.engine import Batch
+    out = []
+    for i, r in enumerate(reqs):
+        C, R, P, B = len(r.Ms), len(r.Ds[0]), r.Ds[0][0].shape[0], r.q ** r.b
+        if C * R * P * B > max_entries:
+            continue
+        locq = np.asarray(r.locq, dtype=np.int64)
+        Ds = [np.vstack(d) for d in r.Ds]
+        clean = O.closed_form_bins(r.Ms, Ds, locq, r.strengths, r.q)
+        nu = r.noise_sd / np.sqrt(2 * B)
+        noise = np.random.RandomState(seed + i).normal(0, nu, clean.shape + (2,)).view(np.complex128)[..., 0] \
+            if nu > 0 else np.zeros_like(clean)
+        sp = r.spec()
+        sp.noise_nu = 0.0                                  # no device noise: the host's is added below
+        bt = Batch([sp], precision=precision, device=dev)
+        bt.eval()
+        bt.gwht()
+        got_bins = bt.job_U(0).cpu().numpy()
+        bins_err = float(np.max(np.abs(got_bins - clean)) / max(np.max(np.abs(clean)), 1e-300))
+        if nu > 0:
+            bt.add_bins(0, torch.from_numpy(noise))
+        bt.peel()
+        keys, vals, _, ctrl = bt.results()[0]
+        got = _key_dict(keys, vals)
+        gw, _, iters = O.peel([clean[c] + noise[c] for c in range(C)], r.Ms, Ds, r.q, r.n, r.b, r.cutoff, r.chan,
+                              r.src, P)
+        want = {tuple(int(x) for x in k): complex(v) for k, v in gw.items()}
+        true = _key_dict(locq.T, r.strengths)
+        same = set(got) == set(want)
+        num = sum(abs(got[k] - want[k]) ** 2 for k in want) if same else float("nan")
+        den = sum(abs(v) ** 2 for v in want.values())
+        out.append({"index": i, "q": r.q, "n": r.n, "b": r.b, "S": r.S, "noisy": bool(nu > 0),
+                    "same_support": bool(same), "same_iterations": int(ctrl.iter) == int(iters),
+                    "coef_rel_l2": float(np.sqrt(num / den)) if den > 0 else 0.0,
+                    "nmse_gpu": O.nmse(true, got), "nmse_oracle": O.nmse(true, want), "bins_rel_err": bins_err})
+    return out
+
+
+def pin_summary(recs):
+    noisy = [x for x in recs if x["noisy"]]
+    rel = [abs(x["nmse_gpu"] - x["nmse_oracle"]) / x["nmse_oracle"] for x in noisy if x["nmse_oracle"] > 0]
+    return {"requests": len(recs), "same_support": f"{sum(x['same_support'] for x in recs)}/{len(recs)}",
+            "same_iterations": f"{sum(x['same_iterations'] for x in recs)}/{len(recs)}",
+            "max_coef_rel_l2": float(max([x["coef_rel_l2"] for x in recs], default=0.0)),
+            "max_bins_rel_err": float(max([x["bins_rel_err"] for x in recs], default=0.0)),
+            "max_nmse_rel_diff_noisy": float(max(rel, default=0.0)),
+            "worst_nmse_oracle": float(max([x["nmse_oracle"] for x in recs], default=0.0))}
+
+
 # DRAM bytes per launch from one ncu capture of this workload (dram__bytes_read.sum +
 # dram__bytes_write.sum; profiles/eval_gemm_q4n20b7_batch16.md, profiles/gwht_row_q4n20b7_batch16.md)
 NCU_TRAFFIC = {"eval": (35.07e6 + 203.33e6) + (12.94e6 + 12.53e6), "gwht": 267.81e6 + 216.15e6, "batch": 16}
 
 
 def run_reference(args):
+    """The reference arm: the reference's CPU algorithm (restated in oracle/) on
+    the host cores, `--steps` whole transforms, each timed (warm-up: `--warmup`
+    transforms of the small noiseless q=4, n=10, b=4 case, untimed)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    vals = []
-    info = None
-    for i in range(max(args.steps, 1)):
-        v, cores, sample = cpu_baseline(sample_rows=SAMPLE_ROWS, seed=args.seed + i)
-        vals.append(v)
-        info = (cores, sample)
-    value = float(np.mean(vals))
+    rec = cpu_transforms(max(args.steps, 1), args.warmup, args.seed)
+    cb = cpu_baseline_record(rec)
+    value = cb["value"]
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / value, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+        "steps": len(rec["step_s"]), "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(rec["step_s"])),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
         "config": {"workload": "q4_n20_b7_C3_nso_R2_S1000_10dB", **WORKLOAD, "batch": 1,
                    "parallelism": "cpu host threads"},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": info[0], "kind": "port", "sample": info[1]},
+        "cpu_baseline": cb,
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
@@ -212,14 +264,36 @@ def run_serving(args, dev):
     lat = rep.percentiles((50, 99))
     sizes = [len(idx) for _, idx, _ in rep.batches]
     # accuracy on the mix, by SNR class: NMSE against the true coefficients
-    by_snr = {}
-    for r, res in zip(reqs, rep.results):
+    by_snr, nm = {}, {}
+    for i, (r, res) in enumerate(zip(reqs, rep.results)):
         if res is None:
             continue
         key = "inf" if r.noise_sd == 0 else "noisy"
-        by_snr.setdefault(key, []).append(coef_nmse(res.keys, res.values, r))
+        nm[i] = coef_nmse(res.keys, res.values, r)
+        by_snr.setdefault(key, []).append(nm[i])
     acc = {k: {"median": float(np.median(v)), "p99": float(np.percentile(v, 99)),
                "frac_le_1e-4": float(np.mean(np.array(v) <= 1e-4))} for k, v in by_snr.items()}
+    # pin to the oracle: the first 50 requests whose bins fit the oracle's size
+    # cap, plus the 5 noisy and 5 noiseless ones of worst NMSE among those that
+    # fit, each with host-drawn noise on both sides (pin_vs_oracle)
+    cap = 1 << 22
+
+    def fits(r):
+        return len(r.Ms) * len(r.Ds[0]) * r.Ds[0][0].shape[0] * r.q ** r.b <= cap
+    fit = [i for i in range(N) if i in nm and fits(reqs[i])]
+    pick = fit[:50]
+    for noisy in (True, False):
+        cls = sorted((i for i in fit if (reqs[i].noise_sd > 0) == noisy), key=lambda i: -nm[i])
+        pick += [i for i in cls[:5] if i not in pick]
+    t = time.perf_counter()
+    recs = pin_vs_oracle([reqs[i] for i in pick], dev, max_entries=cap)
+    for x in recs:
+        x["index"] = pick[x["index"]]
+    pin = pin_summary(recs)
+    pin["seconds"] = time.perf_counter() - t
+    pin["worst"] = sorted(recs, key=lambda x: -x["nmse_oracle"])[:5]
+    pin["selection"] = ("first 50 mix requests with C*R*P*q^b <= 2^22, plus the 5 noisy and 5 noiseless of worst "
+                        "NMSE (in the timed mix) among those; host-drawn noise on both sides")
     # FP64 plain: one request at a time, eager, results read back
     n64 = min(N, 200)
     agree, t64 = 0, 0.0
@@ -242,7 +316,7 @@ def run_serving(args, dev):
             "fp64_plain": {"value": fp64_tps, "unit": UNIT, "sample": n64,
                            "same_support_as_fp32_mix": f"{agree}/{n64}"},
             "batched_fp32_over_fp64_plain": tps / fp64_tps,
-            "nmse_vs_truth": acc, "request_generation_s": t_gen,
+            "nmse_vs_truth": acc, "oracle_pin": pin, "request_generation_s": t_gen,
             "mix": "q{2,3,4,5,20} n[8,60] b[3,8] 40<=q^b<=2^20 S[10,min(2000,q^b/4)] SNR{10,20,inf}dB; "
                    "noisy: NSO R=2, noiseless: identity R=1; C=3"}
 
@@ -302,8 +376,15 @@ def run_ours(args):
                 acc[k] += ev[k][0].elapsed_time(ev[k][1])
 
     batch.capture()                         # one CUDA graph per step
+    # a second workspace with the same inputs: the timed steps alternate between
+    # the two on two streams, two batches in flight as in the end-to-end run
+    batch2 = Batch([r.spec() for r in reqs], precision=args.precision, device=dev)
+    batch2.capture()
+    streams = (torch.cuda.Stream(dev), torch.cuda.Stream(dev))
+    pair = (batch, batch2)
     for _ in range(max(args.warmup, 3)):
         batch.run()
+        batch2.run()
     barrier()
     # clocks: sampled every 50 ms from an untimed ~0.4 s run of the same step
     # just before the timed steps until their end (the K timed steps alone are
@@ -315,14 +396,28 @@ def run_ours(args):
             batch.run()
         torch.cuda.synchronize()
     barrier()
+    # serial replays on one stream (kept for comparison)
     t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     t0e.record(stream)
     for _ in range(args.steps):
         batch.run()
     t1e.record(stream)
     barrier()
-    launches = batch.launches_per_run() * args.steps   # library kernels the timed replays ran
-    dev_ms = t0e.elapsed_time(t1e)
+    serial_ms = max_over_ranks(t0e.elapsed_time(t1e))
+    # the headline: steps alternate between the two workspaces on two streams
+    # (step i waits for step i-2 on its own stream only), CUDA events from a
+    # start event both streams wait on to the later of their end events
+    t0e, ends = torch.cuda.Event(enable_timing=True), [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    t0e.record(stream)
+    for s in streams:
+        s.wait_event(t0e)
+    for i in range(args.steps):
+        pair[i % 2].run(streams[i % 2])
+    for e, s in zip(ends, streams):
+        e.record(s)
+    barrier()
+    launches = sum(pair[i % 2].launches_per_run() for i in range(args.steps))   # library kernels the replays ran
+    dev_ms = max(t0e.elapsed_time(e) for e in ends)
     clocks = clk.stop()
     dev_ms = max_over_ranks(dev_ms)
     value = J * args.steps * world / (dev_ms / 1e3)
@@ -444,6 +539,9 @@ def run_ours(args):
         "config": {"workload": "q4_n20_b7_C3_nso_R2_S1000_10dB", **WORKLOAD, "batch": J,
                    "parallelism": f"replicas x{world}", "l2": "inputs > L2 (bins %.0f MB/step)" %
                    (samples * 8 * J / 1e6)},
+        "value_note": "inputs resident on the device; steps alternate between two captured workspaces on two "
+                      "streams (two batches in flight, the overlap e2e also has)",
+        "value_serial_replay": J * args.steps * world / (serial_ms / 1e3),
         "latency_ms": {"p50": float(np.percentile(lat, 50) * 1e3), "p99": float(np.percentile(lat, 99) * 1e3),
                        "note": "batch completion latency through transform_batch"},
         "phase_ms": phase_ms,
@@ -461,8 +559,7 @@ def run_ours(args):
     if serving is not None:
         line["serving_mix"] = serving
     if not args.no_cpu_baseline:
-        v, cores, sample = cpu_baseline(sample_rows=SAMPLE_ROWS, seed=args.seed)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample}
+        line["cpu_baseline"] = cpu_baseline_record(cpu_transforms(2, 1, args.seed))
     print(json.dumps(line), flush=True)
     RP.shutdown()
 

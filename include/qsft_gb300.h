@@ -108,7 +108,8 @@ typedef struct qsft_ctrl {
 typedef struct qsft_plan {
   int32_t njobs;
   int32_t prec;                /* QSFT_F32 or QSFT_F64                              */
-  int32_t kstride;             /* bytes per decoded-k row in kbuf / ball_k (>= n)   */
+  int32_t kstride;             /* bytes per decoded-k row in kbuf / ball_k (>= n;
+                                * >= 2n with a coded source, qsft_workspace_layout) */
   int32_t flags;               /* QSFT_PLAN_* bits                                  */
   int64_t total_bins;          /* sum of C*B over jobs                              */
   int64_t total_slots;         /* sum of table_cap over jobs                        */
@@ -318,7 +319,10 @@ int qsft_peel_run(const qsft_plan* plan, int max_iter, qsft_stream_t stream);
  * qsft/qsft.py:247-255).  Results of job j are written contiguously:
  * out_index[2j] = first row, out_index[2j+1] = count; rows hold k in
  * out_k[row*kstride ..] (n bytes used), the mean in out_val[2*row .. 2*row+1]
- * and the number of singleton detections averaged in out_cnt[row].
+ * and the number of singleton detections averaged in out_cnt[row].  For a
+ * job with a coded source, k entry i is out_k[.. + i] + q * out_k[.. + n + i]:
+ * the reference keeps a decoded error value outside GF(q) as an entry >= q
+ * (see qsft_rs_decode); every other job has zeros there.
  * *out_total (device int64) receives the row count (the call zeroes it first).
  * Output capacity: plan->total_balls rows.
  */
@@ -330,16 +334,19 @@ int qsft_collect(const qsft_plan* plan, uint8_t* out_k, double* out_val, int32_t
  * Replaces ReedSolomon.syndrome_decode (qsft/ReedSolomon.py:26-48) for nrows
  * syndromes at once: syms[row*2ts ..] holds the 2ts q-ary channel symbols of a
  * row (2t GF(q^s) syndromes, MSB-first digits); k_out[row*n ..] receives the
- * error values on the last n code positions (zero on a decoding failure).
+ * error values on the last n code positions as the integer form of their
+ * GF(q^s) elements (sum of coefficient c_m times q^m), like the reference,
+ * whose k has entries >= q for values outside GF(q); zero on a decoding
+ * failure.
  * gf_tables: exp | log | zech tables of GF(q^s) (the layout qsft_job.rs_gf_off
  * points at).
  */
 int qsft_rs_decode(int q, int s, int t, int n, const int32_t* gf_tables, const uint8_t* syms,
-                   int64_t nrows, uint8_t* k_out, qsft_stream_t stream);
+                   int64_t nrows, int16_t* k_out, qsft_stream_t stream);
 
 /* ---- peeling without device allocation ------------------------------------ */
 #define QSFT_NOALLOC_MAX_BINS 16384  /* largest C * q^b of a qsft_peel_noalloc job       */
-#define QSFT_NOALLOC_KSTRIDE 32      /* out_k row bytes; the job's n must be <= 32        */
+#define QSFT_NOALLOC_KSTRIDE 32      /* out_k row bytes: n <= 32 (n <= 16, coded source)  */
 /*
  * No counterpart in the reference: the peeling loop of qsft_peel_init +
  * qsft_peel_run + qsft_collect for ONE job, for callers that cannot allocate
@@ -358,7 +365,8 @@ int qsft_rs_decode(int q, int s, int t, int n, const int32_t* gf_tables, const u
  * the loop has ended: out_ctrl->err != 0 (QSFT_ERR_OVERFLOW) means a device
  * table filled up and the results are incomplete; iter, n_balls and
  * num_peeling are those of the workspace path.  Limits: C*q^b <=
- * QSFT_NOALLOC_MAX_BINS, n <= 32, else QSFT_ERR_TOO_LARGE.  Every call shares
+ * QSFT_NOALLOC_MAX_BINS and k rows of at most QSFT_NOALLOC_KSTRIDE bytes (n <=
+ * 32; n <= 16 for a coded source), else QSFT_ERR_TOO_LARGE.  Every call shares
  * the one array and its contents stay from the last call: calls that overlap
  * on the GPU race; serialise them.  The first call on a device looks up the
  * array's address with that device current; make it before any stream
@@ -369,9 +377,11 @@ int qsft_peel_noalloc(int prec, const qsft_job* job, const int8_t* i8, void* U, 
                       qsft_ctrl* out_ctrl, qsft_stream_t stream);
 
 /*
- * Scratch sizes for a batch: given the jobs' (q, n, b, C, B) on the host,
- * writes the counts of bins, hash slots, balls and the kstride, and fills the
- * per-job offsets off_bin / off_slot / off_ball, table_cap and ball_cap.
+ * Scratch sizes for a batch: given the jobs' (q, n, b, C, B, src) on the host,
+ * writes the counts of bins, hash slots, balls and the kstride (the k row
+ * bytes: n, or 2n for a coded source, rounded up to 16, largest over the
+ * jobs), and fills the per-job offsets off_bin / off_slot / off_ball,
+ * table_cap and ball_cap.
  */
 int qsft_workspace_layout(qsft_job* jobs_host, int njobs, int64_t* total_bins,
                           int64_t* total_slots, int64_t* total_balls, int32_t* kstride);

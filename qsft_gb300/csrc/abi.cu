@@ -50,16 +50,16 @@ __global__ void collect_kernel(qsft_plan plan, uint8_t* out_k, double* out_val, 
 }
 
 __global__ void rs_decode_kernel(int q, int s, int t, int n, const int32_t* gf_tables, const uint8_t* syms,
-                                 int64_t nrows, uint8_t* k_out) {
+                                 int64_t nrows, int16_t* k_out) {
   const int64_t row = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (row >= nrows) return;
   const GFt g = make_gf(gf_tables, q, s);
   uint8_t sy[256];
-  uint8_t k[QSFT_MAX_N];
+  uint8_t k[QSFT_MAX_N], khi[QSFT_MAX_N];
   const int ns = 2 * t * s;
   for (int i = 0; i < ns; ++i) sy[i] = syms[row * ns + i];
-  rs_decode(g, q, s, t, n, sy, k);
-  for (int i = 0; i < n; ++i) k_out[row * n + i] = k[i];
+  rs_decode(g, q, s, t, n, sy, k, khi);
+  for (int i = 0; i < n; ++i) k_out[row * n + i] = (int16_t)(k[i] + q * khi[i]);
 }
 
 static int64_t next_pow2(int64_t v) {
@@ -127,7 +127,7 @@ extern "C" int qsft_workspace_layout(qsft_job* jobs, int njobs, int64_t* total_b
                                      int64_t* total_balls, int32_t* kstride) {
   if (!jobs || njobs <= 0 || !total_bins || !total_slots || !total_balls || !kstride) return QSFT_ERR_ARG;
   int64_t bins = 0, slots = 0, balls = 0;
-  int maxn = 1;
+  int maxw = 1;  // k row bytes: n digits, and n high parts after them for a coded source
   for (int i = 0; i < njobs; ++i) {
     qsft_job& j = jobs[i];
     if (j.q < 2 || j.q > QSFT_MAX_Q || j.n < 1 || j.n > QSFT_MAX_N || j.b < 1 || j.C < 1 || j.R < 1 || j.P < 2 ||
@@ -158,12 +158,13 @@ extern "C" int qsft_workspace_layout(qsft_job* jobs, int njobs, int64_t* total_b
     bins += cb;
     slots += j.table_cap;
     balls += j.ball_cap;
-    if (j.n > maxn) maxn = j.n;
+    const int w = j.src == QSFT_SRC_CODED ? 2 * j.n : j.n;
+    if (w > maxw) maxw = w;
   }
   *total_bins = bins;
   *total_slots = slots;
   *total_balls = balls;
-  *kstride = (int32_t)(((maxn + 15) / 16) * 16);
+  *kstride = (int32_t)(((maxw + 15) / 16) * 16);
   return QSFT_OK;
 }
 
@@ -180,7 +181,7 @@ extern "C" int qsft_collect(const qsft_plan* plan, uint8_t* out_k, double* out_v
 }
 
 extern "C" int qsft_rs_decode(int q, int s, int t, int n, const int32_t* gf_tables, const uint8_t* syms,
-                              int64_t nrows, uint8_t* k_out, qsft_stream_t stream) {
+                              int64_t nrows, int16_t* k_out, qsft_stream_t stream) {
   if (q < 2 || q > QSFT_MAX_Q || s < 1 || t < 1 || t > QSFT_MAX_RS_T || n < 1 || n > QSFT_MAX_N || nrows < 0)
     return QSFT_ERR_ARG;
   if (2 * t * s > 256) return QSFT_ERR_TOO_LARGE;

@@ -9,7 +9,8 @@
 // g_scratch below, a statically sized device array that every GPU loading
 // this library holds until the process exits.
 //
-// Limits: C*B <= QSFT_NOALLOC_MAX_BINS bins and n <= QSFT_NOALLOC_KSTRIDE.
+// Limits: C*B <= QSFT_NOALLOC_MAX_BINS bins and k rows of at most
+// QSFT_NOALLOC_KSTRIDE bytes (n <= 32; n <= 16 for a coded source).
 // Every call shares the array, and it keeps the last call's contents:
 // qsft_peel_init clears what must start at zero, and calls that overlap on
 // the GPU (different streams, threads or processes' contexts on one device)
@@ -107,7 +108,7 @@ extern "C" int qsft_peel_noalloc(int prec, const qsft_job* job_in, const int8_t*
   int32_t ks = 0;
   const int rc0 = qsft_workspace_layout(&job, 1, &bins, &slots, &balls, &ks);
   if (rc0 != QSFT_OK) return rc0;
-  if (bins > MAX_BINS || slots > MAX_SLOTS || balls > MAX_BALLS || job.n > KSTRIDE) return QSFT_ERR_TOO_LARGE;
+  if (bins > MAX_BINS || slots > MAX_SLOTS || balls > MAX_BALLS || ks > KSTRIDE) return QSFT_ERR_TOO_LARGE;
   if (max_out < job.ball_cap) return QSFT_ERR_ARG;  // output rows the collection may write
   if (job.src == QSFT_SRC_CODED && !gf_tables) return QSFT_ERR_ARG;
   unsigned char* base = nullptr;

@@ -216,7 +216,7 @@ constexpr int DEC_G = 8;
 constexpr int DEC_CPW = 32 / DEC_G;                    // bins per warp at a time
 constexpr int DEC_BINS = DEC_THREADS / DEC_G;          // bins per block at a time
 constexpr int DEC_STAGE_RP = 64;
-constexpr int DEC_KB = QSFT_MAX_N + 16;
+constexpr int DEC_KB = 2 * QSFT_MAX_N;   // k row: n digits mod q, then n high parts for a coded source
 constexpr int PEEL_THREAD_MIN = 1024;  // peel items of a job at least this many: one thread per item
 
 template <typename V>
@@ -331,12 +331,13 @@ __global__ void __launch_bounds__(DEC_THREADS, sizeof(T) == 4 ? 6 : 4) decode_ke
       }
       __syncwarp();
       // ---- source decoding
-      if (job->src == QSFT_SRC_CODED && active && gi == 0) {
+      const bool coded = job->src == QSFT_SRC_CODED;
+      if (coded && active && gi == 0) {
         const GFt g = make_gf(plan.gf_tables + job->rs_gf_off, q, job->rs_s);
-        rs_decode(g, q, job->rs_s, job->rs_t, n, syms, kl);
+        rs_decode(g, q, job->rs_s, job->rs_t, n, syms, kl, kl + n);
       }
       __syncwarp();
-      for (int i = n + gi; i < ks; i += DEC_G) kl[i] = 0;
+      for (int i = (coded ? 2 * n : n) + gi; i < ks; i += DEC_G) kl[i] = 0;
       __syncwarp();
       // ---- projection rho = <omega^(Dk), col> / RP and residual energy, rows
       //      dealt over the group: FP32 for FP32 plans (FP64 within 1% of the
@@ -793,7 +794,7 @@ static int check_plan(const qsft_plan* p) {
       !p->uniq || !p->ball_tab || !p->ball_k || !p->ball_sum || !p->ball_cnt ||
       !p->ctrl || !p->roots || !p->bin_status || !p->bin_stamp || !p->dirty || !p->cand || !p->done_count)
     return QSFT_ERR_ARG;
-  if (p->kstride < 16 || (p->kstride & 15) || p->kstride > QSFT_MAX_N + 16) return QSFT_ERR_ARG;
+  if (p->kstride < 16 || (p->kstride & 15) || p->kstride > 2 * QSFT_MAX_N) return QSFT_ERR_ARG;
   if (p->max_q > QSFT_MAX_Q || p->max_n > QSFT_MAX_N) return QSFT_ERR_TOO_LARGE;
   if (p->prec != QSFT_F32 && p->prec != QSFT_F64) return QSFT_ERR_ARG;
   if (p->total_bins <= 0) return QSFT_ERR_ARG;

@@ -37,11 +37,18 @@ __device__ __forceinline__ int gf_pow_alpha(const GFt& g, int k) {
 // Syndrome decoding of a primitive narrow-sense RS[q^s-1, q^s-1-2t] code
 // (qsft/ReedSolomon.py:26-48): Berlekamp-Massey, Chien search, Forney.
 // syms: 2ts q-ary symbols (MSB-first digits of the 2t syndromes).  On success
-// writes the error values on the last n positions into k; a failure or a
-// value outside GF(q) leaves k = 0 (the all-zero received word).
-static __device__ void rs_decode(const GFt& g, int q, int s, int t, int n, const uint8_t* syms, uint8_t* k) {
+// the error value v on each of the last n positions is written as
+// k[i] = v mod q and khi[i] = v / q, v being the integer form of the GF(q^s)
+// element (sum of its coefficients c_m q^m).  The reference returns v itself
+// (np.array of the decoded field elements, qsft/reconstruct.py:34-51), so a
+// value outside GF(q) gives a k entry >= q: it behaves as v mod q in every
+// later computation (signatures and bin indices are taken mod q) but is a key
+// of its own; khi keeps that key.  v < q^s and q^(s-1) <= n, so khi < 128.
+// A decoding failure leaves k = khi = 0 (the all-zero received word).
+static __device__ void rs_decode(const GFt& g, int q, int s, int t, int n, const uint8_t* syms, uint8_t* k,
+                                 uint8_t* khi) {
   constexpr int CAP = 2 * QSFT_MAX_RS_T + 2;
-  for (int i = 0; i < n; ++i) k[i] = 0;
+  for (int i = 0; i < n; ++i) k[i] = khi[i] = 0;
   int S[2 * QSFT_MAX_RS_T];
   bool any = false;
   for (int j = 0; j < 2 * t; ++j) {
@@ -102,7 +109,7 @@ static __device__ void rs_decode(const GFt& g, int q, int s, int t, int n, const
     om[i] = acc;
   }
   const int nt = g.ord1;
-  uint8_t kk[QSFT_MAX_N];
+  int16_t kk[QSFT_MAX_N];
   for (int i = 0; i < n; ++i) kk[i] = 0;
   for (int r = 0; r < nroots; ++r) {
     const int dg = roots[r];
@@ -122,12 +129,12 @@ static __device__ void rs_decode(const GFt& g, int q, int s, int t, int n, const
     if (den == 0) return;
     const int val = gf_neg(g, gf_mul(g, num, gf_inv(g, den)));  // c = 1: X^(1-c) = 1
     const int pos = nt - 1 - dg;
-    if (pos >= nt - n) {
-      if (val >= q) return;  // not in GF(q): treated as a decoding failure
-      kk[pos - (nt - n)] = (uint8_t)val;
-    }
+    if (pos >= nt - n) kk[pos - (nt - n)] = (int16_t)val;
   }
-  for (int i = 0; i < n; ++i) k[i] = kk[i];
+  for (int i = 0; i < n; ++i) {
+    k[i] = (uint8_t)(kk[i] % q);
+    khi[i] = (uint8_t)(kk[i] / q);
+  }
 }
 
 // Table layout at `tb` (built by the host): exp[2*(q^s-1)] | log[q^s] | zech[q^s-1].

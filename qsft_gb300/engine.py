@@ -204,6 +204,9 @@ class Batch:
         self.gf_host = np.concatenate(gf_parts) if gf_parts else np.zeros(1, np.int32)
         self.njobs = J
         self.shapes = [(sp.q, sp.n, sp.b, sp.C, sp.R, sp.P, sp.S, sp.B) for sp in specs]
+        # coded sources keep each k entry's high part (v // q of a decoded RS
+        # value v outside GF(q)) in the n bytes after the digits of a k row
+        self.coded = [sp.src == "coded" for sp in specs]
         # tensor-core evaluation: K extent, support chunk, work items
         maxn = max(sp.n for sp in specs)
         self.tc_npad = 32 if maxn <= 32 else (64 if maxn <= 64 else 128)
@@ -604,7 +607,10 @@ class Batch:
             if ctrls[j].err:
                 raise _lib.QsftError(f"job {j}: device table overflow during peeling")
             s, c = int(idx[j, 0]), int(idx[j, 1])
-            keys = ks[s:s + c, :shape[1]].astype(np.int64)
+            n = shape[1]
+            keys = ks[s:s + c, :n].astype(np.int64)
+            if self.coded[j]:
+                keys += shape[0] * ks[s:s + c, n:2 * n].astype(np.int64)
             v = vals[s:s + c, 0] + 1j * vals[s:s + c, 1]
             out.append((keys, v, cnts[s:s + c].copy(), ctrls[j]))
         return out
@@ -665,14 +671,16 @@ def eval_points_device(X, K, A, q, precision="fp64"):
 
 
 def rs_decode_batch(rs, syndromes):
-    """Decode rows of 2ts q-ary syndrome symbols on the GPU; returns (rows, n) int64."""
+    """Decode rows of 2ts q-ary syndrome symbols on the GPU; returns (rows, n) int64
+    error values, each the integer form of its GF(q^s) element (>= q outside GF(q),
+    as the reference's ReedSolomon.syndrome_decode returns them)."""
     lib = load()
     dev = torch.device("cuda", torch.cuda.current_device())
     syn = np.ascontiguousarray(np.asarray(syndromes, dtype=np.int64) % rs.q, dtype=np.uint8)
     nrows = syn.shape[0]
     gf = torch.from_numpy(rs.gf_tables()).to(dev)
     sy = torch.from_numpy(syn).to(dev)
-    out = torch.zeros(max(nrows * rs.ns, 1), dtype=torch.uint8, device=dev)
+    out = torch.zeros(max(nrows * rs.ns, 1), dtype=torch.int16, device=dev)
     check(lib.qsft_rs_decode(rs.q, rs.s, rs.t, rs.ns, ctypes.c_void_p(gf.data_ptr()), ctypes.c_void_p(sy.data_ptr()),
                              nrows, ctypes.c_void_p(out.data_ptr()), stream_handle()), "qsft_rs_decode")
     return out[:nrows * rs.ns].cpu().numpy().reshape(nrows, rs.ns).astype(np.int64)

@@ -1,6 +1,6 @@
 """Host side of bench.py on CPU: the reference arm's JSON line (the oracle on
-the host cores, a bounded sample), the coefficient NMSE and the parsing of the
-clock record."""
+the host cores, whole transforms each timed), the coefficient NMSE and the
+parsing of the clock record."""
 import json
 import subprocess
 import sys
@@ -28,6 +28,9 @@ def test_reference_arm_prints_one_contract_line():
     assert d["config"]["workload"] == "q4_n20_b7_C3_nso_R2_S1000_10dB"
     cb = d["cpu_baseline"]
     assert cb["kind"] == "port" and cb["cores"] >= 1 and cb["value"] == d["value"] and cb["sample"]
+    # every claimed step was timed: one whole transform per step, the time a real one
+    assert d["steps"] == 1 and len(cb["step_s"]) == 1
+    assert np.isclose(d["ms_per_step"], 1e3 * cb["step_s"][0]) and np.isclose(d["value"], 1.0 / cb["step_s"][0])
     assert d["e2e"] == {"value": d["value"], "unit": d["unit"], "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
 
 

@@ -176,10 +176,74 @@ def test_rs_decode_vs_oracle(cuda):
             else:            # arbitrary syndromes (multiton bins)
                 syn = rng.randint(0, q, size=2 * t * rs.s)
             rows.append(syn)
-            dec = ors.syndrome_decode(list(syn))[0][0]
-            want.append(dec if dec.max(initial=0) < q else np.zeros(n, int))
+            want.append(ors.syndrome_decode(list(syn))[0][0])
         got = rs_decode_batch(rs, np.array(rows))
         assert np.array_equal(got, np.array(want)), (n, t, q)
+
+
+def test_rs_decode_values_outside_gf_q(cuda):
+    """Syndromes built from error values in GF(q^s) but not in GF(q) (weight <=
+    t, on the last n positions): the decoder returns those values as integers
+    >= q, as ReedSolomon.syndrome_decode does (qsft/ReedSolomon.py:46-48,
+    -dec_codeword[:, -ns:] of galois field elements)."""
+    from qsft_gb300 import ReedSolomon
+    from qsft_gb300.engine import rs_decode_batch
+    rng = np.random.RandomState(2)
+    for (n, t, q) in [(20, 1, 5), (40, 2, 5), (30, 3, 3), (100, 8, 5)]:
+        rs = ReedSolomon(n, t, q)
+        ors = O.rs.ReedSolomonOracle(n, t, q)
+        gf, s = ors.gf, ors.s
+        rows, want = [], []
+        for _ in range(100):
+            e = np.zeros(n, int)
+            w = rng.randint(1, t + 1)
+            e[rng.choice(n, w, replace=False)] = rng.randint(q, q ** s, size=w)   # outside GF(q)
+            syn = []
+            for j in range(2 * t):
+                acc = 0
+                for i in np.nonzero(e)[0]:
+                    acc = gf.add(acc, gf.mul(int(e[i]), ors.H(j, i)))
+                syn += gf.vector(acc)
+            rows.append(syn)
+            want.append(e)
+            assert np.array_equal(ors.syndrome_decode(syn)[0][0], e)        # the oracle, as the reference
+        got = rs_decode_batch(rs, np.array(rows))
+        assert np.array_equal(got, np.array(want)), (n, t, q)
+        assert got.max() >= q
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_coded_transform_keeps_keys_outside_gf_q(cuda, prec):
+    """A coded transform in which noisy multiton bins decode to error values
+    outside GF(q): the reference records such a k (entries >= q) as a key of
+    its own and peels it like k mod q.  The GPU result equals the oracle's
+    (which returns the decoded values as the reference does), keys >= q included."""
+    import qsft_gb300 as Q
+    q, n, b, S, t, C, R, snr, seed = 5, 20, 3, 20, 1, 3, 1, 20, 2
+    qa = dict(query_method="complex", num_subsample=C, delays_method_source="coded", subsampling_method="qsft",
+              delays_method_channel="nso", num_repeat=R, b=b, t=t)
+    nsd = O.noise_sd_for_snr(S, snr)
+    np.random.seed(seed)
+    sig = Q.get_random_subsampled_signal(n=n, q=q, sparsity=S, a_min=1, a_max=10, noise_sd=nsd, query_args=dict(qa),
+                                         max_weight=t, precision=prec)
+    res = Q.QSFT(num_subsample=C, num_repeat=R, b=b, reconstruct_method_source="coded",
+                 reconstruct_method_channel="nso", source_decoder=Q.get_reed_solomon_dec(n, t, q)).transform(sig)
+    np.random.seed(seed)
+    osig = O.OracleSignal(n, q, S, 1, 10, nsd, dict(qa), max_weight=t)
+    calls = {"outside": 0}
+    dec = O.rs.get_reed_solomon_dec(n, t, q)
+
+    def counting(syn):
+        out = dec(syn)
+        calls["outside"] += int(out[0].max(initial=0) >= q)
+        return out
+    ores = O.OracleQSFT(num_subsample=C, num_repeat=R, b=b, reconstruct_method_source="coded",
+                        reconstruct_method_channel="nso", source_decoder=counting).transform(osig)
+    want = {tuple(int(x) for x in k): v for k, v in ores.items()}
+    assert calls["outside"] > 0 and any(max(k) >= q for k in want)
+    assert set(res) == set(want)
+    l2 = np.sqrt(sum(abs(res[k] - want[k]) ** 2 for k in want) / sum(abs(v) ** 2 for v in want.values()))
+    assert l2 < (1e-10 if prec == "fp64" else 1e-5)
 
 
 @pytest.mark.parametrize("prec", PRECS)
@@ -389,16 +453,29 @@ def test_transform_batch_replays_new_inputs(cuda):
 @pytest.mark.parametrize("prec", PRECS)
 def test_config4_coded_full_size(cuda, prec):
     """q=5, n=100, b=5, C=3, RS-coded delays t=8, S=200 of Hamming weight <= 8,
-    20 dB: the RS path has no reference run (galois), so ground truth."""
+    20 dB, at full size: the oracle on the same seed (same signal, query design,
+    permutation and host noise) gives the same support and coefficients
+    (relative L2 1e-5 FP32, 1e-10 FP64), and both recover the true support."""
+    import os
     import qsft_gb300 as Q
     q, n, b, S, t = 5, 100, 5, 200, 8
     qa = dict(query_method="complex", num_subsample=3, delays_method_source="coded", subsampling_method="qsft",
               delays_method_channel="nso", num_repeat=1, b=b, t=t)
+    nsd = O.noise_sd_for_snr(S, 20)
     np.random.seed(0)
-    sig = Q.get_random_subsampled_signal(n=n, q=q, sparsity=S, a_min=1, a_max=10, noise_sd=O.noise_sd_for_snr(S, 20),
-                                         query_args=qa, max_weight=t, precision=prec)
+    sig = Q.get_random_subsampled_signal(n=n, q=q, sparsity=S, a_min=1, a_max=10, noise_sd=nsd,
+                                         query_args=dict(qa), max_weight=t, precision=prec)
     res = Q.QSFT(num_subsample=3, num_repeat=1, b=b, reconstruct_method_source="coded", reconstruct_method_channel="nso",
                  source_decoder=Q.get_reed_solomon_dec(n, t, q)).transform(sig, report=True)
+    np.random.seed(0)
+    osig = O.OracleSignal(n, q, S, 1, 10, nsd, dict(qa), max_weight=t, eval_threads=os.cpu_count() or 1)
+    ores = O.OracleQSFT(num_subsample=3, num_repeat=1, b=b, reconstruct_method_source="coded",
+                        reconstruct_method_channel="nso",
+                        source_decoder=O.rs.get_reed_solomon_dec(n, t, q)).transform(osig)
+    want = {tuple(int(x) for x in k): v for k, v in ores.items()}
+    assert set(res["gwht"]) == set(want)
+    l2 = np.sqrt(sum(abs(res["gwht"][k] - want[k]) ** 2 for k in want) / sum(abs(v) ** 2 for v in want.values()))
+    assert l2 < (1e-10 if prec == "fp64" else 1e-5), l2
     assert set(res["gwht"]) == set(sig.signal_w)
     assert O.nmse(sig.signal_w, res["gwht"]) < 1e-4
     assert res["n_samples"] == 3 * sig.get_source_parity() * q ** b
