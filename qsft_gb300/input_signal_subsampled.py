@@ -141,16 +141,25 @@ class SubsampledSignal(Signal):
 
     def _subsample_qsft(self):
         """Sample every coset and take the sub-transforms for each b in all_bs
-        (qsft/input_signal_subsampled.py:107-155, 264-266), on the GPU."""
+        (qsft/input_signal_subsampled.py:107-155, 264-266), on the GPU.
+
+        With a folder, the reference's cache files are read and written:
+        ``transforms/U{i}_{j}.pickle`` holds (Us[i][j], transformTimes[i][j]) --
+        {b: (P, q^b) complex array}, {b: seconds} -- and
+        ``samples/M{i}_D{j}.pickle`` the (P, q^b) samples of group i, repeat j
+        (zlib pickles, qsft/utils.py:189-197).  A folder the reference filled
+        is thus reused, and the reference can reuse one filled here."""
         C, R = len(self.Ms), len(self.Ds[0])
         cached = self._load_transforms()
         if cached is not None:
-            self._bins = cached
-            self.transformTimes = [[{b: 0.0 for b in self.all_bs} for _ in range(R)] for _ in range(C)]
+            self._bins, self.transformTimes = cached
             return
-        samples = self._sample_device()
+        samples = self._load_samples()
         if samples is None:
-            samples = self._sample_host()
+            samples = self._sample_device()
+            if samples is None:
+                samples = self._sample_host()
+            self._save_samples(samples)
         P = samples.shape[2]
         bins = {}
         times = {}
@@ -172,21 +181,63 @@ class SubsampledSignal(Signal):
         self.transformTimes = [[dict(times) for _ in range(R)] for _ in range(C)]
         self._save_transforms()
 
+    def _cache_path(self, kind, i, j):
+        if kind == "transforms":
+            return Path(f"{self.foldername}/transforms/U{i}_{j}.pickle")   # qsft/input_signal_subsampled.py:122
+        return Path(f"{self.foldername}/samples/M{i}_D{j}.pickle")         # qsft/input_signal_subsampled.py:128
+
     def _load_transforms(self):
+        """Every (group, repeat) from transforms/U{i}_{j}.pickle when all files
+        exist and hold every b of all_bs; else None."""
         if not self.foldername:
             return None
-        paths = {b: Path(f"{self.foldername}/transforms/U_b{b}.pt") for b in self.all_bs}
-        if not all(p.is_file() for p in paths.values()):
+        C, R = len(self.Ms), len(self.Ds[0])
+        paths = [[self._cache_path("transforms", i, j) for j in range(R)] for i in range(C)]
+        if not all(p.is_file() for row in paths for p in row):
+            return None
+        data = [[load_data(p) for p in row] for row in paths]
+        if not all(b in d[0] for row in data for d in row for b in self.all_bs):
             return None
         dev = torch.device("cuda", torch.cuda.current_device())
-        return {b: torch.load(p, map_location=dev) for b, p in paths.items()}
+        cdt = complex_dtype(precision_code(self.precision))
+        bins = {b: torch.from_numpy(np.stack([np.stack([np.asarray(d[0][b], dtype=np.complex128) for d in row])
+                                              for row in data])).to(dev).to(cdt) for b in self.all_bs}
+        times = [[dict(d[1]) for d in row] for row in data]
+        return bins, times
 
     def _save_transforms(self):
         if not self.foldername:
             return
         Path(f"{self.foldername}/transforms").mkdir(exist_ok=True, parents=True)
-        for b, t in self._bins.items():
-            torch.save(t.cpu(), f"{self.foldername}/transforms/U_b{b}.pt")
+        host = {b: t.cpu().numpy().astype(np.complex128) for b, t in self._bins.items()}
+        for i in range(len(self.Ms)):
+            for j in range(len(self.Ds[i])):
+                save_data(({b: host[b][i, j] for b in host}, dict(self.transformTimes[i][j])),
+                          self._cache_path("transforms", i, j))
+
+    def _load_samples(self):
+        """(C, R, P, q^b) device samples from samples/M{i}_D{j}.pickle when every
+        file exists; else None."""
+        if not self.foldername:
+            return None
+        C, R = len(self.Ms), len(self.Ds[0])
+        paths = [[self._cache_path("samples", i, j) for j in range(R)] for i in range(C)]
+        if not all(p.is_file() for row in paths for p in row):
+            return None
+        arr = np.stack([np.stack([np.asarray(load_data(p), dtype=np.complex128) for p in row]) for row in paths])
+        dev = torch.device("cuda", torch.cuda.current_device())
+        return torch.from_numpy(arr).to(dev).to(complex_dtype(precision_code(self.precision)))
+
+    def _save_samples(self, samples):
+        if not self.foldername:
+            return
+        Path(f"{self.foldername}/samples").mkdir(exist_ok=True, parents=True)
+        host = samples.cpu().numpy().astype(np.complex128)
+        for i in range(host.shape[0]):
+            for j in range(host.shape[1]):
+                p = self._cache_path("samples", i, j)
+                if not p.is_file():
+                    save_data(host[i, j], p)
 
     def _subsample_uniform(self):  # qsft/input_signal_subsampled.py:157-173
         import random

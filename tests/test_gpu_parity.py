@@ -501,6 +501,75 @@ def test_folder_cache_round_trip(cuda, tmp_path):
     assert max(abs(out[0][k] - out[1][k]) for k in out[0]) < 1e-6
 
 
+def _ref_save(obj, path):
+    """The reference's cache writer (qsft/utils.py:189-192): zlib level 9 of a pickle."""
+    import pickle
+    import zlib
+    path.parent.mkdir(parents=True, exist_ok=True)
+    path.write_bytes(zlib.compress(pickle.dumps(obj, pickle.HIGHEST_PROTOCOL), 9))
+
+
+def _ref_load(path):
+    import pickle
+    import zlib
+    return pickle.loads(zlib.decompress(path.read_bytes()))
+
+
+@pytest.mark.parametrize("prec", PRECS)
+def test_folder_in_reference_format(cuda, tmp_path, prec):
+    """A folder laid out as the reference fills it -- Ms_and_Ds.pickle,
+    transforms/U{i}_{j}.pickle = (Us[i][j], transformTimes[i][j]) with
+    Us[i][j] = {b: (P, q^b) bins} (qsft/input_signal_subsampled.py:92-155) --
+    is loaded without sampling, and the transform gives the oracle's result on
+    those bins; a folder filled here has the same files and contents."""
+    import qsft_gb300 as Q
+    q, n, b, S, C, R = 4, 10, 4, 30, 3, 2
+    qa = dict(query_method="complex", num_subsample=C, delays_method_source="identity", subsampling_method="qsft",
+              delays_method_channel="nso", num_repeat=R, b=b)
+    np.random.seed(21)
+    osig = O.OracleSignal(n, q, S, 1, 10, 0.5, dict(qa))
+    ref_dir = tmp_path / "ref"
+    _ref_save((osig.Ms, osig.Ds), ref_dir / "Ms_and_Ds.pickle")
+    for i in range(C):
+        for j in range(R):
+            _ref_save(({b: osig.Us[i][j]}, {b: 0.01}), ref_dir / "transforms" / f"U{i}_{j}.pickle")
+
+    class NoSampling(Q.SyntheticSubsampledSignal):
+        def _sample_device(self):
+            raise AssertionError("the cached transforms must be used")
+
+    np.random.seed(21)
+    _, locq, strengths = Q.generate_signal_w(n, q, S, 1, 10, full=False)
+    sig = NoSampling(signal_w=None, locq=locq, strengths=strengths, noise_sd=0.5, n=n, q=q, query_args=dict(qa),
+                     folder=str(ref_dir), precision=prec)
+    np.random.seed(5)
+    got = Q.QSFT(num_subsample=C, num_repeat=R, b=b, reconstruct_method_source="identity",
+                 reconstruct_method_channel="nso").transform(sig)
+    np.random.seed(5)
+    want = O.OracleQSFT(num_subsample=C, num_repeat=R, b=b, reconstruct_method_source="identity",
+                        reconstruct_method_channel="nso").transform(osig)
+    want = {tuple(int(x) for x in k): v for k, v in want.items()}
+    assert set(got) == set(want) and len(want) >= 25
+    assert max(abs(got[k] - want[k]) / abs(want[k]) for k in want) < (1e-10 if prec == "fp64" else 1e-5)
+    assert sig.transformTimes[0][0][b] == 0.01
+    # written here: the reference's files, same layout and values
+    out_dir = tmp_path / "ours"
+    np.random.seed(21)
+    mine = Q.get_random_subsampled_signal(n=n, q=q, sparsity=S, a_min=1, a_max=10, noise_sd=0.5, query_args=dict(qa),
+                                          folder=str(out_dir), precision=prec)
+    Ms, Ds = _ref_load(out_dir / "Ms_and_Ds.pickle")
+    assert all(np.array_equal(x, y) for x, y in zip(Ms, osig.Ms))
+    for i in range(C):
+        for j in range(R):
+            us, ts = _ref_load(out_dir / "transforms" / f"U{i}_{j}.pickle")
+            assert set(us) == {b} and set(ts) == {b} and us[b].shape == (n + 1, q ** b)
+            assert us[b].dtype == np.complex128
+            assert rel_err(us[b], osig.Us[i][j]) < REL[prec]
+            smp = _ref_load(out_dir / "samples" / f"M{i}_D{j}.pickle")
+            assert smp.shape == (n + 1, q ** b)
+    assert mine._bins[b].shape == (C, R, n + 1, q ** b)
+
+
 def test_generic_plugin_subsample(cuda):
     """A user SubsampledSignal that only implements subsample(query_indices) on
     the host: sub-transforms and peeling on the GPU give the synthetic path's result."""
