@@ -196,6 +196,42 @@ def pin_vs_oracle(reqs, dev, precision="fp32", seed=123, max_entries=1 << 22):
     return out
 
 
+def pin_own_inputs(batch, req):
+    """The timed workload's own inputs through the oracle, for job 0 of the
+    batch: (1) the step's evaluation + GWHT without noise against the oracle's
+    closed-form bins; (2) the step as timed (evaluation, GWHT with the device
+    Philox noise fused), its noisy bins read back before the peeling, then the
+    oracle's peeling (FP64 numpy restatement of qsft/qsft.py:151-255) on
+    exactly those bins against the GPU's peeling of them."""
+    import oracle as O
+    sp = batch.specs[0]
+    C, RP = sp.C, sp.R * sp.P
+    Ds = [np.vstack(d) for d in req.Ds]
+    clean = O.closed_form_bins(req.Ms, Ds, np.asarray(req.locq, dtype=np.int64), req.strengths, req.q)
+    batch.eval()
+    batch.gwht()
+    got = batch.job_U(0).cpu().numpy()
+    bins_err = float(np.max(np.abs(got - clean)) / np.max(np.abs(clean)))
+    batch.eval()
+    batch.gwht_noise()
+    noisy = batch.job_U(0).cpu().numpy().astype(np.complex128)
+    batch.peel()
+    keys, vals, _, ctrl = batch.results()[0]
+    gpu = _key_dict(keys, vals)
+    gw, _, iters = O.peel([noisy[c].copy() for c in range(C)], req.Ms, Ds, req.q, req.n, req.b, req.cutoff, req.chan,
+                          req.src, sp.P)
+    want = {tuple(int(x) for x in k): complex(v) for k, v in gw.items()}
+    same = set(gpu) == set(want)
+    l2 = float(np.sqrt(sum(abs(gpu[k] - want[k]) ** 2 for k in want) / sum(abs(v) ** 2 for v in want.values()))) \
+        if same and want else float("nan")
+    resid = noisy - clean
+    nu = req.noise_sd / np.sqrt(2 * req.q ** req.b)
+    return {"job": 0, "clean_bins_rel_err_vs_closed_form": bins_err, "same_support": bool(same),
+            "same_iterations": int(ctrl.iter) == int(iters), "coef_rel_l2_vs_oracle": l2,
+            "noise_std_over_nu": float(np.std(np.concatenate([resid.real.ravel(), resid.imag.ravel()])) / nu),
+            "note": "the bench's own device-noise bins of transform 0, peeled by the oracle (FP64) and by the GPU"}
+
+
 def pin_summary(recs):
     noisy = [x for x in recs if x["noisy"]]
     rel = [abs(x["nmse_gpu"] - x["nmse_oracle"]) / x["nmse_oracle"] for x in noisy if x["nmse_oracle"] > 0]
@@ -489,6 +525,7 @@ def run_ours(args):
     nmse64 = coef_nmse(k64, v64, reqs[0])
     same_support = set(map(tuple, k64.tolist())) == set(map(tuple, res[0][0].tolist()))
 
+    own = pin_own_inputs(batch, reqs[0])
     serving = run_serving(args, dev) if args.serve_requests > 0 else None
 
     if rank != 0:
@@ -551,7 +588,8 @@ def run_ours(args):
                      "nmse_limit": 1e-4,
                      "transform0": {"nmse_fp32_batched": nmse32[0], "nmse_fp64_plain": nmse64,
                                     "nmse_rel_diff": abs(nmse32[0] - nmse64) / max(nmse64, 1e-300),
-                                    "same_support": bool(same_support)}},
+                                    "same_support": bool(same_support)},
+                     "oracle_on_own_inputs": own},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "roofline": roofline, "roofline_gwht": roof_gwht, "clocks": clocks,

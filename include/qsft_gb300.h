@@ -96,7 +96,7 @@ typedef struct qsft_ctrl {
   int32_t n_unique;            /* distinct balls peeled in the current iteration    */
   int32_t n_balls;             /* distinct balls recorded so far (result size)      */
   int32_t err;                 /* QSFT_ERR_OVERFLOW when a table filled up          */
-  int32_t n_cand;              /* bins above the energy cutoff queued for decoding  */
+  int32_t n_cand;              /* bins above the energy cutoff in this iteration    */
   int32_t n_dirty[2];          /* bins changed by the peel of an iteration (parity) */
   int64_t num_peeling;         /* cumulative balls peeled                           */
 } qsft_ctrl;
@@ -108,7 +108,7 @@ typedef struct qsft_ctrl {
 typedef struct qsft_plan {
   int32_t njobs;
   int32_t prec;                /* QSFT_F32 or QSFT_F64                              */
-  int32_t kstride;             /* bytes per decoded-k row in kbuf / ball_k (>= n;
+  int32_t kstride;             /* bytes per k row in ball_k and the outputs (>= n;
                                 * >= 2n with a coded source, qsft_workspace_layout) */
   int32_t flags;               /* QSFT_PLAN_* bits                                  */
   int64_t total_bins;          /* sum of C*B over jobs                              */
@@ -127,7 +127,6 @@ typedef struct qsft_plan {
   const int32_t* gf_tables;    /* RS: exp | log | zech tables per field             */
   const double* roots;         /* exp(2 pi i m / q) at ((q*32 + m)*2), q <= 32      */
   /* peeling workspace (sizes from qsft_workspace_layout) */
-  uint8_t* kbuf;               /* [total_bins * kstride] decoded k per singleton bin */
   double* rho;                 /* [total_bins * 2]   FP64 coefficient per singleton bin */
   /* persistent hash table k -> ball: (tag << 32) | (ball id + 1), tag a
    * nonzero 32-bit hash of k, so that probes compare k rows only on a tag hit */
@@ -144,9 +143,10 @@ typedef struct qsft_plan {
   uint8_t* bin_status;         /* [total_bins] 0 zeroton, 1 multiton, 2 singleton  */
   int32_t* bin_stamp;          /* [total_bins] last iteration that changed the bin  */
   int32_t* dirty;              /* [2 * total_bins] changed bins, by iteration parity */
-  int32_t* cand;               /* [total_bins] bins queued for decoding             */
-  int32_t* done_count;         /* [1] jobs whose loop has ended (peel kernels exit
-                                * at once when it reaches njobs)                    */
+  int32_t* done_count;         /* [2]: [0] jobs whose loop has ended (the peeling
+                                * kernels exit at once when it reaches njobs);
+                                * [1] blocks of the running peel launch that have
+                                * finished (the last one closes the iteration)     */
   /* tensor-core evaluation (FP32 plans): work items are (job, support chunk of
    * tc_smax entries, group of QSFT_TC_TILES tiles of 128 samples)              */
   const int64_t* tc_prefix;    /* [njobs+1] cumulative work items, or NULL          */
@@ -302,8 +302,9 @@ int qsft_peel_init(const qsft_plan* plan, qsft_stream_t stream);
  * function of the bin's unchanged values, so the outcome is the same.
  */
 int qsft_peel_iteration(const qsft_plan* plan, int first, qsft_stream_t stream);
-/* kernels one peeling iteration launches (scan, decode, record, peel, iter_end) */
-#define QSFT_PEEL_LAUNCHES_PER_ITER 5
+/* kernels one peeling iteration launches (detect: zeroton test, decoding and
+ * recording of singletons; peel: subtraction and the iteration's end) */
+#define QSFT_PEEL_LAUNCHES_PER_ITER 2
 /*
  * Up to max_iter iterations.  Issued eagerly, all max_iter are launched
  * (iterations of finished jobs are no-ops).  Inside a stream capture,
@@ -355,7 +356,7 @@ int qsft_rs_decode(int q, int s, int t, int n, const int32_t* gf_tables, const u
  * applications that own every buffer (a fixed memory budget or a pool of
  * their own) and hand a library only its inputs and outputs.  All scratch
  * (hash tables, result store, lists, roots table, control record) lives in a
- * statically sized device array inside the library (about 2.4 MB, held by
+ * statically sized device array inside the library (about 1.8 MB, held by
  * every GPU that loads the library until the process exits), so the call
  * allocates nothing.  `job` is a host record (offsets off_M/off_D into i8,
  * off_U into U; qsft_workspace_layout's fields are filled in by the call); U

@@ -23,7 +23,7 @@ TC_TILE_M = 128
 NOALLOC_MAX_BINS = 16384   # QSFT_NOALLOC_MAX_BINS
 NOALLOC_KSTRIDE = 32       # QSFT_NOALLOC_KSTRIDE
 TC_SUB_N = 128
-PEEL_LAUNCHES_PER_ITER = 5   # QSFT_PEEL_LAUNCHES_PER_ITER
+PEEL_LAUNCHES_PER_ITER = 2   # QSFT_PEEL_LAUNCHES_PER_ITER
 
 # exported symbols, in header order
 SYMBOLS = [
@@ -77,9 +77,9 @@ class QsftPlan(ctypes.Structure):
         ("max_rp", ctypes.c_int32),
         ("jobs", _P), ("eval_prefix", _P), ("bin_prefix", _P), ("i8", _P), ("A", _P), ("U", _P),
         ("gf_tables", _P), ("roots", _P),
-        ("kbuf", _P), ("rho", _P), ("ball_tab", _P), ("ball_best", _P), ("uniq", _P),
+        ("rho", _P), ("ball_tab", _P), ("ball_best", _P), ("uniq", _P),
         ("ball_k", _P), ("ball_sum", _P), ("ball_cnt", _P), ("ctrl", _P),
-        ("bin_status", _P), ("bin_stamp", _P), ("dirty", _P), ("cand", _P), ("done_count", _P),
+        ("bin_status", _P), ("bin_stamp", _P), ("dirty", _P), ("done_count", _P),
         ("tc_prefix", _P), ("total_tc_work", ctypes.c_int64), ("tc_smax", ctypes.c_int32),
         ("tc_npad", ctypes.c_int32), ("min_q", ctypes.c_int32), ("tc_table_bytes", ctypes.c_int32),
         ("tc_entry_bytes", ctypes.c_int32), ("pad2_", ctypes.c_int32), ("status", _P),

@@ -38,8 +38,7 @@ constexpr size_t OFF_ROOTS = al(OFF_PREFIX + 2 * sizeof(int64_t));
 constexpr size_t OFF_INDEX = al(OFF_ROOTS + 33 * 32 * 2 * sizeof(double));
 constexpr size_t OFF_CTRL = al(OFF_INDEX + 2 * sizeof(int64_t));
 constexpr size_t OFF_DONE = al(OFF_CTRL + sizeof(qsft_ctrl));
-constexpr size_t OFF_KBUF = al(OFF_DONE + sizeof(int32_t));
-constexpr size_t OFF_RHO = al(OFF_KBUF + MAX_BINS * KSTRIDE);
+constexpr size_t OFF_RHO = al(OFF_DONE + 2 * sizeof(int32_t));
 constexpr size_t OFF_BALLTAB = al(OFF_RHO + MAX_BINS * 2 * sizeof(double));
 constexpr size_t OFF_BALLBEST = al(OFF_BALLTAB + MAX_SLOTS * sizeof(int64_t));
 constexpr size_t OFF_UNIQ = al(OFF_BALLBEST + MAX_BALLS * sizeof(int64_t));
@@ -49,8 +48,7 @@ constexpr size_t OFF_BALLCNT = al(OFF_BALLSUM + MAX_BALLS * 2 * sizeof(double));
 constexpr size_t OFF_STATUS = al(OFF_BALLCNT + MAX_BALLS * sizeof(int32_t));
 constexpr size_t OFF_STAMP = al(OFF_STATUS + MAX_BINS);
 constexpr size_t OFF_DIRTY = al(OFF_STAMP + MAX_BINS * sizeof(int32_t));
-constexpr size_t OFF_CAND = al(OFF_DIRTY + 2 * MAX_BINS * sizeof(int32_t));
-constexpr size_t TOTAL = al(OFF_CAND + MAX_BINS * sizeof(int32_t));
+constexpr size_t TOTAL = al(OFF_DIRTY + 2 * MAX_BINS * sizeof(int32_t));
 
 // the scratch: held by every GPU that loads the library, shared by every call
 static __device__ __align__(256) unsigned char g_scratch[TOTAL];
@@ -135,7 +133,6 @@ extern "C" int qsft_peel_noalloc(int prec, const qsft_job* job_in, const int8_t*
   p.U = U;
   p.gf_tables = gf_tables;
   p.roots = reinterpret_cast<const double*>(base + OFF_ROOTS);
-  p.kbuf = base + OFF_KBUF;
   p.rho = reinterpret_cast<double*>(base + OFF_RHO);
   p.ball_tab = reinterpret_cast<int64_t*>(base + OFF_BALLTAB);
   p.ball_best = reinterpret_cast<int64_t*>(base + OFF_BALLBEST);
@@ -147,7 +144,6 @@ extern "C" int qsft_peel_noalloc(int prec, const qsft_job* job_in, const int8_t*
   p.bin_status = base + OFF_STATUS;
   p.bin_stamp = reinterpret_cast<int32_t*>(base + OFF_STAMP);
   p.dirty = reinterpret_cast<int32_t*>(base + OFF_DIRTY);
-  p.cand = reinterpret_cast<int32_t*>(base + OFF_CAND);
   p.done_count = reinterpret_cast<int32_t*>(base + OFF_DONE);
 
   // qsft_peel_init zeroes everything that must start at zero (control record,

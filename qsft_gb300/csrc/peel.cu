@@ -1,31 +1,29 @@
 // Singleton detection and peeling: QSFT.transform's while-loop
 // (qsft/qsft.py:151-255) for a batch of transforms.
 //
-// One iteration = five launches:
-//   scan          thread per bin: the zeroton test ||col||^2 > cutoff*len
-//                 (qsft/qsft.py:164); bins above it are queued.  The first
-//                 iteration scans every bin; later ones only the bins that the
-//                 previous subtractions changed (the rest keep their class:
-//                 it is a function of the bin's unchanged values), and the
-//                 multiton count is kept up to date as classes change.
-//   decode        a group of 8 threads per queued bin: channel decoding of k (noiseless
-//                 qsft/reconstruct.py:12-31 or NSO "nso1" :100-113, lanes over
-//                 symbols), optional Reed-Solomon source decoding (:34-51),
-//                 projection rho = <omega^(Dk), col>/len and residual energy
-//                 (lanes over rows, warp reductions), bin-match test
-//                 (qsft/qsft.py:174-190); singletons leave k and rho behind.
-//   record        thread per queued bin: each singleton finds (or creates)
-//                 the ball of its k in a persistent hash table, adds its rho to
-//                 the ball's running sum (the `result` list and its mean,
-//                 :217, 247-255) and marks the ball detected in this iteration
-//                 keeping the largest (group, bin) -- the reference's dict
-//                 order, `ball_values` (:209-216).
-//   peel          per (detected ball, group l) -- a thread, or 8 for short lists: subtract
-//                 rho * omega^(D_l k) from bin M_l^T k (mod q) of group l
-//                 (qsft/qsft.py:223-241) and queue the changed bin for the
-//                 next scan.
-//   iter_end      per job: iteration count, cumulative peel count and the
-//                 loop's stopping rules (qsft/qsft.py:151, 204-205).
+// One iteration = two launches:
+//   detect   a warp takes 32 bins at a time (the first iteration: every bin,
+//            consecutive bins of a group, coalesced; later ones: the bins the
+//            previous subtractions changed -- the others keep their class, a
+//            function of their unchanged values).  Lane per bin: the zeroton
+//            test ||col||^2 > cutoff*len (qsft/qsft.py:164); the warp's
+//            candidates are then decoded four at a time by groups of 8 lanes
+//            while their columns are still in L2: channel decoding of k
+//            (noiseless qsft/reconstruct.py:12-31 or NSO "nso1" :100-113),
+//            optional Reed-Solomon source decoding (:34-51), projection
+//            rho = <omega^(Dk), col>/len and residual energy, bin-match test
+//            (qsft/qsft.py:174-190).  Each singleton is recorded at once:
+//            it finds (or creates) the ball of its k in a persistent hash
+//            table, adds rho to the ball's running sum (the `result` list and
+//            its mean, :217, 247-255) and marks the ball detected in this
+//            iteration keeping the largest (group, bin) -- the reference's
+//            dict order, `ball_values` (:209-216).
+//   peel     per (detected ball, group l) -- a thread, or 8 for short lists:
+//            subtract rho * omega^(D_l k) from bin M_l^T k (mod q) of group l
+//            (qsft/qsft.py:223-241) and queue the changed bin for the next
+//            detect.  The block that finishes last closes the iteration for
+//            every job: iteration count, cumulative peel count and the loop's
+//            stopping rules (qsft/qsft.py:151, 204-205).
 //
 // FP32 data path: bins are stored as float2.  Energy, phase and residual
 // decisions that fall within a small band of their thresholds are recomputed
@@ -35,11 +33,9 @@
 
 namespace qsft {
 
-constexpr int SCAN_THREADS = 256;
-constexpr int WARPS_PER_BLOCK = 8;
+constexpr int PEEL_THREADS = 256;
 constexpr int MAX_SYMS = 256;  // channel symbols per bin (P - 1 <= 256)
 constexpr int LIST_BLOCKS = 152 * 8;
-constexpr int DEC_BLOCKS = 152 * 12;
 
 // ---------------------------------------------------------------- helpers
 __device__ __forceinline__ uint32_t hash_row(const uint8_t* row, int words) {
@@ -84,10 +80,18 @@ __device__ __forceinline__ double warp_sum(double v) {
 // ||col||^2 with the FP64 recomputation band of the FP32 path
 template <typename T>
 __device__ __forceinline__ double col_energy(const c2<T>* col, int RP, int B, double thr) {
+  // the loads of 16 rows are issued before their sum (in row order) is taken:
+  // a lane keeps 16 independent loads in flight instead of a few
+  constexpr int BATCH = 16;
   T e = 0;
-  for (int r = 0; r < RP; ++r) {
-    const c2<T> v = col[(int64_t)r * B];
-    e += v.x * v.x + v.y * v.y;
+  for (int r0 = 0; r0 < RP; r0 += BATCH) {
+    c2<T> v[BATCH];
+#pragma unroll
+    for (int k = 0; k < BATCH; ++k)
+      if (r0 + k < RP) v[k] = col[(int64_t)(r0 + k) * B];
+#pragma unroll
+    for (int k = 0; k < BATCH; ++k)
+      if (r0 + k < RP) e += v[k].x * v[k].x + v[k].y * v[k].y;
   }
   double E = (double)e;
   if (sizeof(T) == 4 && fabs(E - thr) <= 1e-3 * thr) {
@@ -111,71 +115,7 @@ __device__ __forceinline__ int warp_append(bool want, int jid, int* counter) {
   return base + __popc(mask & ((1u << lane) - 1));
 }
 
-// ---------------------------------------------------------------- scan
-// first iteration: every bin of every active job
-template <typename T>
-__global__ void __launch_bounds__(SCAN_THREADS) scan_all_kernel(qsft_plan plan) {
-  const int64_t gb = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const bool inrange = gb < plan.total_bins;
-  const int jid = find_job(plan.bin_prefix, plan.njobs, inrange ? gb : plan.total_bins - 1);
-  const qsft_job* __restrict__ job = plan.jobs + jid;
-  qsft_ctrl* ctl = plan.ctrl + jid;
-  const int B = job->B, RP = job->R * job->P;
-  const int local = (int)(gb - job->off_bin);
-  bool cand = false;
-  if (inrange && !ctl->done) {
-    const int c = local / B, jb = local - (local / B) * B;
-    const c2<T>* col = reinterpret_cast<const c2<T>*>(plan.U) + job->off_U + (int64_t)c * RP * B + jb;
-    const double thr = job->cutoff * RP;
-    cand = col_energy<T>(col, RP, B, thr) > thr;
-    plan.bin_status[gb] = 0;
-  }
-  const int pos = warp_append(cand, jid, &ctl->n_cand);
-  if (cand) plan.cand[job->off_bin + pos] = local;
-}
-
-// later iterations: the bins the previous iteration's subtractions changed
-template <typename T>
-__global__ void __launch_bounds__(SCAN_THREADS) scan_dirty_kernel(qsft_plan plan) {
-  if (__ldcg(plan.done_count) >= plan.njobs) return;  // every job has left the loop
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int gw = tid >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-  int64_t chunk0 = 0;  // 32-entry chunks of all jobs' lists are dealt round-robin to the warps
-  for (int jid = 0; jid < plan.njobs; ++jid) {
-    qsft_ctrl* ctl = plan.ctrl + jid;
-    if (ctl->done) continue;
-    const int parity = (ctl->iter) & 1;  // written by the peel of iteration `iter`
-    const int cnt = ctl->n_dirty[parity];
-    const int nch = (cnt + 31) >> 5;
-    const int start = (int)(((int64_t)gw - chunk0) % nw + nw) % nw;
-    chunk0 += nch;
-    if (start >= nch) continue;
-    const qsft_job* __restrict__ job = plan.jobs + jid;
-    const int B = job->B, RP = job->R * job->P;
-    const double thr = job->cutoff * RP;
-    const int32_t* list = plan.dirty + (int64_t)parity * plan.total_bins + job->off_bin;
-    // all threads of a warp iterate together so that warp_append sees full warps
-    for (int ch = start; ch < nch; ch += nw) {
-      const int i = ch * 32 + (tid & 31);
-      bool cand = false;
-      int local = 0;
-      if (i < cnt) {
-        local = list[i];
-        const int64_t gb = job->off_bin + local;
-        if (plan.bin_status[gb] == 1) atomicSub(&ctl->n_multi, 1);
-        plan.bin_status[gb] = 0;
-        const int c = local / B, jb = local - (local / B) * B;
-        const c2<T>* col = reinterpret_cast<const c2<T>*>(plan.U) + job->off_U + (int64_t)c * RP * B + jb;
-        cand = col_energy<T>(col, RP, B, thr) > thr;
-      }
-      const int pos = warp_append(cand, jid, &ctl->n_cand);
-      if (cand) plan.cand[job->off_bin + pos] = local;
-    }
-  }
-}
-
 // ---------------------------------------------------------------- decode
-constexpr int STAGE_RP = 128;  // columns of up to this many rows are staged in shared memory
 
 // phase <d, k> mod q of delay row d (n digits) against k (kstride-padded bytes)
 __device__ __forceinline__ int row_phase(const int8_t* dr, const uint8_t* kl, int n, bool words_ok, int q) {
@@ -202,15 +142,13 @@ __device__ __forceinline__ bool krow_eq(const uint8_t* mine, const uint8_t* othe
   return eq;
 }
 
-// A group of DEC_G threads per queued bin (DEC_G consecutive lanes; a warp
-// holds 32 / DEC_G bins): symbols, rows and digits are dealt over the group
-// and its sums reduced with in-group shuffles, so every bin of an iteration
-// is in flight at once (first iteration: ~50K bins) while the dependent chain
-// of one bin stays short (later iterations: a few thousand).  A warp works on
-// bins of one job (chunks dealt round-robin), so control flow is uniform.
-// The column's RP values (stride B in U) are staged in shared memory with one
-// round of loads when RP <= DEC_STAGE_RP; FP32 roots for every q come from a
-// block-wide table.
+// A candidate bin is decoded by a group of DEC_G threads (DEC_G consecutive
+// lanes; a warp holds 32 / DEC_G bins): symbols, rows and digits are dealt
+// over the group and its sums reduced with in-group shuffles, so the dependent
+// chain of one bin stays short.  A warp works on bins of one job (chunks dealt
+// round-robin), so control flow is uniform.  The column's RP values (stride B
+// in U) are staged in shared memory with one round of loads when
+// RP <= DEC_STAGE_RP; FP32 roots for every q come from a block-wide table.
 constexpr int DEC_THREADS = 128;
 constexpr int DEC_G = 8;
 constexpr int DEC_CPW = 32 / DEC_G;                    // bins per warp at a time
@@ -232,9 +170,80 @@ __device__ __forceinline__ V group_sum_g(V v, unsigned mask, int g) {
   return v;
 }
 
+// n-th (from 0) set bit of m, n < popc(m)
+__device__ __forceinline__ int nth_set(unsigned m, int n) {
+  for (int i = 0; i < n; ++i) m &= m - 1;
+  return __ffs(m) - 1;
+}
+
+// ---------------------------------------------------------------- record
+// One singleton (k in the 16-byte aligned row kr, coefficient rho) of bin
+// `local`: find (or create) the ball of its k in the job's persistent table
+// (tags first, k rows only on a tag hit), add rho to the ball's running sum,
+// and mark the ball detected in this iteration with (iteration << 32 | local)
+// by atomicMax -- the largest local bin wins, the reference's last-write order
+// over (group, bin) (qsft/qsft.py:209-216).  Returns the ball id (-1 when a
+// table is full: ctrl.err) and whether this is the ball's first detection in
+// the iteration (the old value's iteration field tells).
+__device__ __forceinline__ int record_one(const qsft_plan& plan, const qsft_job* __restrict__ job, qsft_ctrl* ctl,
+                                          const uint8_t* kr, int local, double2 rho, long long iter, int ks,
+                                          bool& first) {
+  first = false;
+  const int64_t mask = job->table_cap - 1;
+  unsigned long long* tab = reinterpret_cast<unsigned long long*>(plan.ball_tab + job->off_slot);
+  const uint32_t h = hash_row(kr, ks / 4);
+  const unsigned long long tag = (unsigned long long)(h | 1u) << 32;
+  int64_t slot = h & mask;
+  int myid = -1, bid = -1;
+  for (int64_t probe = 0; probe < job->table_cap; ++probe) {
+    unsigned long long cur = __ldcg(tab + slot);
+    if (cur == 0) {
+      if (myid < 0) {  // publish our k row before the slot that points at it
+        myid = atomicAdd(&ctl->n_balls, 1);
+        if (myid >= job->ball_cap) break;
+        const uint4* src = reinterpret_cast<const uint4*>(kr);
+        uint4* dst = reinterpret_cast<uint4*>(plan.ball_k + (job->off_ball + myid) * ks);
+        for (int w = 0; w < ks / 16; ++w) dst[w] = src[w];
+        __threadfence();
+      }
+      const unsigned long long prev = atomicCAS(tab + slot, 0ull, tag | (unsigned long long)(myid + 1));
+      if (prev == 0) {
+        bid = myid;
+        break;
+      }
+      cur = prev;
+    }
+    if ((cur & 0xffffffff00000000ull) == tag) {
+      const int other = (int)(cur & 0xffffffffull) - 1;
+      if (krow_eq(kr, plan.ball_k + (job->off_ball + other) * ks, ks)) {
+        bid = other;
+        break;
+      }
+    }
+    slot = (slot + 1) & mask;
+  }
+  if (bid < 0) {
+    atomicExch(&ctl->err, (int)QSFT_ERR_OVERFLOW);
+    return -1;
+  }
+  // a ball id allocated for a k that another thread inserted first stays an
+  // empty row (count 0): the collection skips it
+  const int64_t gball = job->off_ball + bid;
+  atomicAdd(plan.ball_sum + 2 * gball, rho.x);
+  atomicAdd(plan.ball_sum + 2 * gball + 1, rho.y);
+  atomicAdd(plan.ball_cnt + gball, 1);
+  const unsigned long long old = atomicMax(reinterpret_cast<unsigned long long*>(plan.ball_best) + gball,
+                                           (unsigned long long)((iter << 32) | (unsigned)local));
+  first = (long long)(old >> 32) != iter;
+  return bid;
+}
+
+// ---------------------------------------------------------------- detect
+constexpr int DET_BLOCKS = 152 * 5;   // resident at once (5 blocks of 128 threads per SM)
+
 template <typename T>
-// FP32: 6 blocks per SM (80 registers, no spill; measured 2% faster than 4)
-__global__ void __launch_bounds__(DEC_THREADS, sizeof(T) == 4 ? 6 : 4) decode_kernel(qsft_plan plan) {
+// FP32: 5 blocks per SM (up to 102 registers: no spill)
+__global__ void __launch_bounds__(DEC_THREADS, sizeof(T) == 4 ? 5 : 4) detect_kernel(qsft_plan plan, int first) {
   if (__ldcg(plan.done_count) >= plan.njobs) return;  // every job has left the loop
   __shared__ float2 s_w[33 * 32];                            // roots, FP32
   __shared__ c2<T> s_col[DEC_BINS][DEC_STAGE_RP];
@@ -250,293 +259,254 @@ __global__ void __launch_bounds__(DEC_THREADS, sizeof(T) == 4 ? 6 : 4) decode_ke
   const int ks = plan.kstride;
   c2<T>* sc = s_col[slot];
   uint8_t* kl = s_k[slot];
-  int64_t chunk0 = 0;
+  int64_t chunk0 = 0;  // 32-bin chunks of all jobs are dealt round-robin to the warps
   for (int jid = 0; jid < plan.njobs; ++jid) {
     qsft_ctrl* ctl = plan.ctrl + jid;
     if (ctl->done) continue;
-    const int cnt = ctl->n_cand;
-    const int nch = (cnt + DEC_CPW - 1) / DEC_CPW;
-    const int start = (int)(((int64_t)gw - chunk0) % nw + nw) % nw;
-    chunk0 += nch;
-    if (start >= nch) continue;
     const qsft_job* __restrict__ job = plan.jobs + jid;
     const int q = job->q, n = job->n, b = job->b, B = job->B, P = job->P, R = job->R;
     const int RP = R * P, nsym = P - 1;
+    const int parity = ctl->iter & 1;   // the dirty list the peel of iteration `iter` wrote
+    const int cnt = first ? job->C * B : ctl->n_dirty[parity];
+    const int nch = (cnt + 31) >> 5;
+    const int start = (int)(((int64_t)gw - chunk0) % nw + nw) % nw;
+    chunk0 += nch;
+    if (start >= nch) continue;
     const double thr = job->cutoff * RP;
     const bool staged = RP <= DEC_STAGE_RP;
     const bool words_ok = (n & 3) == 0 && ((job->off_D & 3) == 0);
     const float2* wq = s_w + q * 32;
     uint8_t* syms = job->src == QSFT_SRC_CODED ? s_sym[slot] : kl;
+    const long long iter = (long long)ctl->iter + 1;
+    const int32_t* list = plan.dirty + (int64_t)parity * plan.total_bins + job->off_bin;
     for (int ch = start; ch < nch; ch += nw) {   // uniform over the warp: every lane runs every sync
-      const int u = ch * DEC_CPW + lane / DEC_G;
-      const bool active = u < cnt;
-      const int local = active ? plan.cand[job->off_bin + u] : 0;
-      const int c = local / B, jb = local - (local / B) * B;
-      const int64_t gb = job->off_bin + local;
-      const c2<T>* col = reinterpret_cast<const c2<T>*>(plan.U) + job->off_U + (int64_t)c * RP * B + jb;
-      if (staged && active)
-        for (int r = gi; r < RP; r += DEC_G) sc[r] = col[(int64_t)r * B];
-      __syncwarp();
-      auto V = [&](int r) -> c2<T> { return staged ? sc[r] : col[(int64_t)r * B]; };
-      // ---- channel decoding, symbols dealt over the group
-      if (active) {
-        if (job->chan == QSFT_CHAN_IDENTITY) {
-          const c2<T> v0 = V(0);
-          const T a0 = atan2(v0.y, v0.x);
-          for (int i = 1 + gi; i < RP && i <= nsym; i += DEC_G) {
-            const c2<T> vi = V(i);
-            const T ai = atan2(vi.y, vi.x);
-            double a = (double)((T)q * (ai - a0) / (T)6.283185307179586);
-            if (sizeof(T) == 4 && fabs(a - floor(a) - 0.5) < 1e-3)
-              a = (double)q * (atan2((double)vi.y, (double)vi.x) - atan2((double)v0.y, (double)v0.x)) /
-                  6.283185307179586;
-            long long m = (long long)rint(a);  // round half to even, like np.round
-            m %= q;
-            if (m < 0) m += q;
-            syms[i - 1] = (uint8_t)m;
-          }
-        } else {
-          for (int i = 1 + gi; i <= nsym; i += DEC_G) {
-            T zr = 0, zi = 0;
-            for (int r = 0; r < R; ++r) {
-              const c2<T> u0 = V(r * P), ui = V(r * P + i);
-              zr += u0.x * ui.x + u0.y * ui.y;
-              zi += u0.y * ui.x - u0.x * ui.y;
+      // ---- zeroton test, lane per bin
+      const int i = ch * 32 + lane;
+      bool is_cand = false;
+      int mylocal = 0;
+      if (i < cnt) {
+        mylocal = first ? i : list[i];
+        const int64_t gbl = job->off_bin + mylocal;
+        if (!first && plan.bin_status[gbl] == 1) atomicSub(&ctl->n_multi, 1);
+        plan.bin_status[gbl] = 0;
+        const int cc = mylocal / B, jj = mylocal - (mylocal / B) * B;
+        const c2<T>* cl = reinterpret_cast<const c2<T>*>(plan.U) + job->off_U + (int64_t)cc * RP * B + jj;
+        is_cand = col_energy<T>(cl, RP, B, thr) > thr;
+      }
+      const unsigned cmask = __ballot_sync(0xffffffffu, is_cand);
+      const int ncand = __popc(cmask);
+      if (lane == 0 && ncand) atomicAdd(&ctl->n_cand, ncand);
+      __syncwarp();  // the class resets above are ordered before the decode's writes
+      // ---- the candidates, DEC_CPW at a time
+      for (int r0 = 0; r0 < ncand; r0 += DEC_CPW) {
+        const int mine = r0 + lane / DEC_G;
+        const bool active = mine < ncand;
+        const int src_lane = active ? nth_set(cmask, mine) : 0;
+        const int local = __shfl_sync(0xffffffffu, mylocal, src_lane);
+        const int c = local / B, jb = local - (local / B) * B;
+        const int64_t gb = job->off_bin + local;
+        const c2<T>* col = reinterpret_cast<const c2<T>*>(plan.U) + job->off_U + (int64_t)c * RP * B + jb;
+        if (staged && active)
+          for (int r = gi; r < RP; r += DEC_G) sc[r] = col[(int64_t)r * B];
+        __syncwarp();
+        auto V = [&](int r) -> c2<T> { return staged ? sc[r] : col[(int64_t)r * B]; };
+        // ---- channel decoding, symbols dealt over the group
+        if (active) {
+          if (job->chan == QSFT_CHAN_IDENTITY) {
+            const c2<T> v0 = V(0);
+            const T a0 = atan2(v0.y, v0.x);
+            for (int i = 1 + gi; i < RP && i <= nsym; i += DEC_G) {
+              const c2<T> vi = V(i);
+              const T ai = atan2(vi.y, vi.x);
+              double a = (double)((T)q * (ai - a0) / (T)6.283185307179586);
+              if (sizeof(T) == 4 && fabs(a - floor(a) - 0.5) < 1e-3)
+                a = (double)q * (atan2((double)vi.y, (double)vi.x) - atan2((double)v0.y, (double)v0.x)) /
+                    6.283185307179586;
+              long long m = (long long)rint(a);  // round half to even, like np.round
+              m %= q;
+              if (m < 0) m += q;
+              syms[i - 1] = (uint8_t)m;
             }
-            if (sizeof(T) == 4) {
-              float ang = atan2f((float)zi, (float)zr);
-              if (ang < 0.f) ang += 6.28318530717958647f;
-              const float tq = ang * (float)q * 0.15915494309189535f;
-              if (fabsf(tq - floorf(tq) - 0.5f) >= 1e-3f) {
-                // away from a tie the nearest of 2 pi m / q, m = 0..q, is floor(tq + 1/2)
-                syms[i - 1] = (uint8_t)(((int)floorf(tq + 0.5f)) % q);
-                continue;
-              }
-              double dzr = 0, dzi = 0;  // near a rounding boundary: recompute in FP64
+          } else {
+            for (int i = 1 + gi; i <= nsym; i += DEC_G) {
+              T zr = 0, zi = 0;
               for (int r = 0; r < R; ++r) {
-                const double2 u0 = to_d2(V(r * P)), ui = to_d2(V(r * P + i));
-                dzr += u0.x * ui.x + u0.y * ui.y;
-                dzi += u0.y * ui.x - u0.x * ui.y;
+                const c2<T> u0 = V(r * P), ui = V(r * P + i);
+                zr += u0.x * ui.x + u0.y * ui.y;
+                zi += u0.y * ui.x - u0.x * ui.y;
               }
-              double ang64 = atan2(dzi, dzr);
-              if (ang64 < 0) ang64 += 6.283185307179586;
-              syms[i - 1] = (uint8_t)nearest_root(ang64, q);
-            } else {
-              double ang = (double)atan2(zi, zr);
-              if (ang < 0) ang += 6.283185307179586;
-              syms[i - 1] = (uint8_t)nearest_root(ang, q);
+              if (sizeof(T) == 4) {
+                float ang = atan2f((float)zi, (float)zr);
+                if (ang < 0.f) ang += 6.28318530717958647f;
+                const float tq = ang * (float)q * 0.15915494309189535f;
+                if (fabsf(tq - floorf(tq) - 0.5f) >= 1e-3f) {
+                  // away from a tie the nearest of 2 pi m / q, m = 0..q, is floor(tq + 1/2)
+                  syms[i - 1] = (uint8_t)(((int)floorf(tq + 0.5f)) % q);
+                  continue;
+                }
+                double dzr = 0, dzi = 0;  // near a rounding boundary: recompute in FP64
+                for (int r = 0; r < R; ++r) {
+                  const double2 u0 = to_d2(V(r * P)), ui = to_d2(V(r * P + i));
+                  dzr += u0.x * ui.x + u0.y * ui.y;
+                  dzi += u0.y * ui.x - u0.x * ui.y;
+                }
+                double ang64 = atan2(dzi, dzr);
+                if (ang64 < 0) ang64 += 6.283185307179586;
+                syms[i - 1] = (uint8_t)nearest_root(ang64, q);
+              } else {
+                double ang = (double)atan2(zi, zr);
+                if (ang < 0) ang += 6.283185307179586;
+                syms[i - 1] = (uint8_t)nearest_root(ang, q);
+              }
             }
           }
         }
-      }
-      __syncwarp();
-      // ---- source decoding
-      const bool coded = job->src == QSFT_SRC_CODED;
-      if (coded && active && gi == 0) {
-        const GFt g = make_gf(plan.gf_tables + job->rs_gf_off, q, job->rs_s);
-        rs_decode(g, q, job->rs_s, job->rs_t, n, syms, kl, kl + n);
-      }
-      __syncwarp();
-      for (int i = (coded ? 2 * n : n) + gi; i < ks; i += DEC_G) kl[i] = 0;
-      __syncwarp();
-      // ---- projection rho = <omega^(Dk), col> / RP and residual energy, rows
-      //      dealt over the group: FP32 for FP32 plans (FP64 within 1% of the
-      //      threshold), FP64 for FP64 plans
-      const int8_t* Dc = plan.i8 + job->off_D + (int64_t)c * RP * n;
-      auto project64 = [&](double2& rho_out, double& res_out) {
-        double ar = 0, ai = 0;
-        for (int r = gi; r < RP; r += DEC_G) {
-          const double2 w = root(plan.roots, q, row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q));
-          const double2 v = to_d2(V(r));
-          ar += w.x * v.x + w.y * v.y;
-          ai += w.x * v.y - w.y * v.x;
+        __syncwarp();
+        // ---- source decoding
+        const bool coded = job->src == QSFT_SRC_CODED;
+        if (coded && active && gi == 0) {
+          const GFt g = make_gf(plan.gf_tables + job->rs_gf_off, q, job->rs_s);
+          rs_decode(g, q, job->rs_s, job->rs_t, n, syms, kl, kl + n);
         }
-        ar = group_sum(ar, gmask);
-        ai = group_sum(ai, gmask);
-        const double2 rh = make_double2(ar / RP, ai / RP);
-        double rs = 0;
-        for (int r = gi; r < RP; r += DEC_G) {
-          const double2 w = root(plan.roots, q, row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q));
-          const double2 v = to_d2(V(r));
-          const double dx = v.x - (rh.x * w.x - rh.y * w.y);
-          const double dy = v.y - (rh.x * w.y + rh.y * w.x);
-          rs += dx * dx + dy * dy;
-        }
-        rho_out = rh;
-        res_out = group_sum(rs, gmask);
-      };
-      double2 rho = make_double2(0.0, 0.0);
-      double res = 0.0;
-      if (sizeof(T) == 4) {
-        int ph[(DEC_STAGE_RP + DEC_G - 1) / DEC_G];
-        float ar = 0.f, ai = 0.f;
-#pragma unroll
-        for (int k = 0; k < (DEC_STAGE_RP + DEC_G - 1) / DEC_G; ++k) {
-          const int r = gi + k * DEC_G;
-          ph[k] = 0;
-          if (r < RP) {
-            ph[k] = row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q);
-            const float2 w = wq[ph[k]];
+        __syncwarp();
+        for (int i = (coded ? 2 * n : n) + gi; i < ks; i += DEC_G) kl[i] = 0;
+        __syncwarp();
+        // ---- projection rho = <omega^(Dk), col> / RP and residual energy, rows
+        //      dealt over the group: FP32 for FP32 plans (FP64 within 1% of the
+        //      threshold), FP64 for FP64 plans
+        const int8_t* Dc = plan.i8 + job->off_D + (int64_t)c * RP * n;
+        auto project64 = [&](double2& rho_out, double& res_out) {
+          double ar = 0, ai = 0;
+          for (int r = gi; r < RP; r += DEC_G) {
+            const double2 w = root(plan.roots, q, row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q));
+            const double2 v = to_d2(V(r));
+            ar += w.x * v.x + w.y * v.y;
+            ai += w.x * v.y - w.y * v.x;
+          }
+          ar = group_sum(ar, gmask);
+          ai = group_sum(ai, gmask);
+          const double2 rh = make_double2(ar / RP, ai / RP);
+          double rs = 0;
+          for (int r = gi; r < RP; r += DEC_G) {
+            const double2 w = root(plan.roots, q, row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q));
+            const double2 v = to_d2(V(r));
+            const double dx = v.x - (rh.x * w.x - rh.y * w.y);
+            const double dy = v.y - (rh.x * w.y + rh.y * w.x);
+            rs += dx * dx + dy * dy;
+          }
+          rho_out = rh;
+          res_out = group_sum(rs, gmask);
+        };
+        double2 rho = make_double2(0.0, 0.0);
+        double res = 0.0;
+        if (sizeof(T) == 4) {
+          int ph[(DEC_STAGE_RP + DEC_G - 1) / DEC_G];
+          float ar = 0.f, ai = 0.f;
+  #pragma unroll
+          for (int k = 0; k < (DEC_STAGE_RP + DEC_G - 1) / DEC_G; ++k) {
+            const int r = gi + k * DEC_G;
+            ph[k] = 0;
+            if (r < RP) {
+              ph[k] = row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q);
+              const float2 w = wq[ph[k]];
+              const c2<T> v = V(r);
+              ar += w.x * (float)v.x + w.y * (float)v.y;
+              ai += w.x * (float)v.y - w.y * (float)v.x;
+            }
+          }
+          for (int r = gi + DEC_STAGE_RP; r < RP; r += DEC_G) {  // rows past the register-held phases
+            const float2 w = wq[row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q)];
             const c2<T> v = V(r);
             ar += w.x * (float)v.x + w.y * (float)v.y;
             ai += w.x * (float)v.y - w.y * (float)v.x;
           }
-        }
-        for (int r = gi + DEC_STAGE_RP; r < RP; r += DEC_G) {  // rows past the register-held phases
-          const float2 w = wq[row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q)];
-          const c2<T> v = V(r);
-          ar += w.x * (float)v.x + w.y * (float)v.y;
-          ai += w.x * (float)v.y - w.y * (float)v.x;
-        }
-        ar = group_sum(ar, gmask) / (float)RP;
-        ai = group_sum(ai, gmask) / (float)RP;
-        float rs = 0.f;
-#pragma unroll
-        for (int k = 0; k < (DEC_STAGE_RP + DEC_G - 1) / DEC_G; ++k) {
-          const int r = gi + k * DEC_G;
-          if (r < RP) {
-            const float2 w = wq[ph[k]];
+          ar = group_sum(ar, gmask) / (float)RP;
+          ai = group_sum(ai, gmask) / (float)RP;
+          float rs = 0.f;
+  #pragma unroll
+          for (int k = 0; k < (DEC_STAGE_RP + DEC_G - 1) / DEC_G; ++k) {
+            const int r = gi + k * DEC_G;
+            if (r < RP) {
+              const float2 w = wq[ph[k]];
+              const c2<T> v = V(r);
+              const float dx = (float)v.x - (ar * w.x - ai * w.y);
+              const float dy = (float)v.y - (ar * w.y + ai * w.x);
+              rs += dx * dx + dy * dy;
+            }
+          }
+          for (int r = gi + DEC_STAGE_RP; r < RP; r += DEC_G) {
+            const float2 w = wq[row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q)];
             const c2<T> v = V(r);
             const float dx = (float)v.x - (ar * w.x - ai * w.y);
             const float dy = (float)v.y - (ar * w.y + ai * w.x);
             rs += dx * dx + dy * dy;
           }
+          rs = group_sum(rs, gmask);
+          rho = make_double2(ar, ai);
+          res = rs;
+          if (fabsf(rs - (float)thr) <= 1e-2f * (float)thr) project64(rho, res);  // group-uniform
+        } else {
+          project64(rho, res);
         }
-        for (int r = gi + DEC_STAGE_RP; r < RP; r += DEC_G) {
-          const float2 w = wq[row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q)];
-          const c2<T> v = V(r);
-          const float dx = (float)v.x - (ar * w.x - ai * w.y);
-          const float dy = (float)v.y - (ar * w.y + ai * w.x);
-          rs += dx * dx + dy * dy;
+        // ---- bin match: digit t of M_c^T k equals digit t of j (MSB first), digits over the group
+        bool ok = true;
+        {
+          const int8_t* Mc = plan.i8 + job->off_M + (int64_t)c * n * b;
+          for (int t = gi; t < b; t += DEC_G) {
+            int jr = jb;
+            for (int tt = b - 1; tt > t; --tt) jr /= q;
+            int dg = 0;
+            for (int i = 0; i < n; ++i) dg += (int)Mc[i * b + t] * (int)kl[i];
+            ok &= (dg % q) == (jr % q);
+          }
         }
-        rs = group_sum(rs, gmask);
-        rho = make_double2(ar, ai);
-        res = rs;
-        if (fabsf(rs - (float)thr) <= 1e-2f * (float)thr) project64(rho, res);  // group-uniform
-      } else {
-        project64(rho, res);
-      }
-      // ---- bin match: digit t of M_c^T k equals digit t of j (MSB first), digits over the group
-      bool ok = true;
-      {
-        const int8_t* Mc = plan.i8 + job->off_M + (int64_t)c * n * b;
-        for (int t = gi; t < b; t += DEC_G) {
-          int jr = jb;
-          for (int tt = b - 1; tt > t; --tt) jr /= q;
-          int dg = 0;
-          for (int i = 0; i < n; ++i) dg += (int)Mc[i * b + t] * (int)kl[i];
-          ok &= (dg % q) == (jr % q);
-        }
-      }
-      const bool match = (__ballot_sync(0xffffffffu, !ok) & gmask) == 0;
-      const bool single = match && !(res > thr);
-      if (active) {
-        if (single)  // k, rho and the class for the record kernel
-          for (int w = gi; w < ks / 16; w += DEC_G)
-            reinterpret_cast<uint4*>(plan.kbuf + gb * ks)[w] = reinterpret_cast<const uint4*>(kl)[w];
-        if (gi == 0) {
+        const bool match = (__ballot_sync(0xffffffffu, !ok) & gmask) == 0;
+        const bool single = match && !(res > thr);
+        bool firstb = false;
+        int bid = -1;
+        if (active && gi == 0) {
           plan.bin_status[gb] = single ? 2 : 1;
           if (single) {
-            plan.rho[2 * gb] = rho.x;
+            plan.rho[2 * gb] = rho.x;   // the peel reads the coefficient of the ball's last bin
             plan.rho[2 * gb + 1] = rho.y;
+            bid = record_one(plan, job, ctl, kl, local, rho, iter, ks, firstb);
           }
           atomicAdd(single ? &ctl->n_single : &ctl->n_multi, 1);
         }
+        const int pos = warp_append(firstb, jid, &ctl->n_unique);   // the iteration's list of balls
+        if (firstb) plan.uniq[job->off_ball + pos] = bid;
+        __syncwarp();  // the slot's buffers are reused by the next bin
       }
-      __syncwarp();  // the slot's buffers are reused by the next bin
-    }
-  }
-}
-
-// ---------------------------------------------------------------- record
-// Thread per queued bin; singletons (bin_status 2, k in kbuf, rho in rho) are
-// recorded: each finds (or creates) the ball of its k in the persistent table
-// (tags first, k rows only on a tag hit), adds rho to the ball's running sum,
-// and marks the ball detected in this iteration with (iteration << 32 | local)
-// by atomicMax -- the largest local bin wins, the reference's last-write order
-// over (group, bin) (qsft/qsft.py:209-216) -- appending the ball to the
-// iteration's list on its first detection.  A warp works on 32 bins of one
-// job at once, so the table's L2 round trips overlap.
-__global__ void __launch_bounds__(SCAN_THREADS) record_kernel(qsft_plan plan) {
-  if (__ldcg(plan.done_count) >= plan.njobs) return;
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  const int gw = tid >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-  const int ks = plan.kstride;
-  int64_t chunk0 = 0;  // 32-entry chunks of all jobs' lists are dealt round-robin to the warps
-  for (int jid = 0; jid < plan.njobs; ++jid) {
-    qsft_ctrl* ctl = plan.ctrl + jid;
-    if (ctl->done) continue;
-    const int cnt = ctl->n_cand;
-    const int nch = (cnt + 31) >> 5;
-    const int start = (int)(((int64_t)gw - chunk0) % nw + nw) % nw;
-    chunk0 += nch;
-    if (start >= nch) continue;
-    const qsft_job* __restrict__ job = plan.jobs + jid;
-    const long long iter = (long long)ctl->iter + 1;
-    const int64_t mask = job->table_cap - 1;
-    unsigned long long* tab = reinterpret_cast<unsigned long long*>(plan.ball_tab + job->off_slot);
-    for (int ch = start; ch < nch; ch += nw) {
-      const int i = ch * 32 + (tid & 31);
-      bool first = false;
-      int bid = -1;
-      if (i < cnt) {
-        const int local = plan.cand[job->off_bin + i];
-        const int64_t gb = job->off_bin + local;
-        if (plan.bin_status[gb] == 2) {
-          const uint8_t* kr = plan.kbuf + gb * ks;
-          const uint32_t h = hash_row(kr, ks / 4);
-          const unsigned long long tag = (unsigned long long)(h | 1u) << 32;
-          int64_t slot = h & mask;
-          int myid = -1;
-          for (int64_t probe = 0; probe < job->table_cap; ++probe) {
-            unsigned long long cur = __ldcg(tab + slot);
-            if (cur == 0) {
-              if (myid < 0) {  // publish our k row before the slot that points at it
-                myid = atomicAdd(&ctl->n_balls, 1);
-                if (myid >= job->ball_cap) break;
-                const uint4* src = reinterpret_cast<const uint4*>(kr);
-                uint4* dst = reinterpret_cast<uint4*>(plan.ball_k + (job->off_ball + myid) * ks);
-                for (int w = 0; w < ks / 16; ++w) dst[w] = src[w];
-                __threadfence();
-              }
-              const unsigned long long prev = atomicCAS(tab + slot, 0ull, tag | (unsigned long long)(myid + 1));
-              if (prev == 0) {
-                bid = myid;
-                break;
-              }
-              cur = prev;
-            }
-            if ((cur & 0xffffffff00000000ull) == tag) {
-              const int other = (int)(cur & 0xffffffffull) - 1;
-              if (krow_eq(kr, plan.ball_k + (job->off_ball + other) * ks, ks)) {
-                bid = other;
-                break;
-              }
-            }
-            slot = (slot + 1) & mask;
-          }
-          if (bid < 0) {
-            atomicExch(&ctl->err, (int)QSFT_ERR_OVERFLOW);
-          } else {
-            // a ball id allocated for a k that another thread inserted first
-            // stays an empty row (count 0): the collection skips it
-            const int64_t gball = job->off_ball + bid;
-            atomicAdd(plan.ball_sum + 2 * gball, plan.rho[2 * gb]);
-            atomicAdd(plan.ball_sum + 2 * gball + 1, plan.rho[2 * gb + 1]);
-            atomicAdd(plan.ball_cnt + gball, 1);
-            const unsigned long long old = atomicMax(reinterpret_cast<unsigned long long*>(plan.ball_best) + gball,
-                                                     (unsigned long long)((iter << 32) | (unsigned)local));
-            first = (long long)(old >> 32) != iter;
-          }
-        }
-      }
-      const int pos = warp_append(first, jid, &ctl->n_unique);
-      if (first) plan.uniq[job->off_ball + pos] = bid;
     }
   }
 }
 
 // ---------------------------------------------------------------- peel
+// Per job, by one block after every subtraction of the iteration: iteration
+// count, cumulative peel count and the loop's stopping rules (qsft/qsft.py:151,
+// 204-205); the counters of the next iteration start at zero.  *s_iter
+// receives the largest iteration count (the WHILE node's bound).
+__device__ __forceinline__ void end_iteration(const qsft_plan& plan, int* s_iter) {
+  for (int jid = threadIdx.x; jid < plan.njobs; jid += blockDim.x) {
+    volatile qsft_ctrl* ctl = plan.ctrl + jid;
+    const qsft_job* job = plan.jobs + jid;
+    if (ctl->done) continue;
+    const int it = ctl->iter + 1;
+    ctl->iter = it;
+    atomicMax(s_iter, it);
+    ctl->num_peeling = ctl->num_peeling + ctl->n_unique;
+    if (ctl->n_multi == 0 || ctl->n_single == 0 || it >= job->max_iter || ctl->num_peeling >= job->peeling_max ||
+        ctl->err != 0) {
+      ctl->done = 1;
+      atomicAdd(plan.done_count, 1);
+    }
+    ctl->n_single = 0;
+    ctl->n_unique = 0;
+    ctl->n_cand = 0;
+    ctl->n_dirty[(it - 1) & 1] = 0;  // consumed by this iteration's detect
+  }
+}
+
 // one bin-entry subtraction: U -= (dx, dy)
 __device__ __forceinline__ void sub_entry(float2* p, float dx, float dy) {
   asm volatile("red.global.add.v2.f32 [%0], {%1, %2};" ::"l"(p), "f"(-dx), "f"(-dy) : "memory");
@@ -554,8 +524,9 @@ __device__ __forceinline__ void sub_entry(double2* p, double dx, double dy) {
 // cut the latency of each item when there are few to overlap.  FP32 plans
 // rotate rho in FP32 (the entries it is subtracted from are FP32).
 template <typename T>
-__global__ void __launch_bounds__(SCAN_THREADS) peel_kernel(qsft_plan plan) {
-  if (__ldcg(plan.done_count) >= plan.njobs) return;  // every job has left the loop
+__global__ void __launch_bounds__(PEEL_THREADS) peel_kernel(qsft_plan plan, cudaGraphConditionalHandle cond,
+                                                           int set_cond, int max_iter) {
+  if (__ldcg(plan.done_count) >= plan.njobs) return;  // every job has left the loop (the same in every block)
   __shared__ float2 s_w[33 * 32];                     // FP32 roots, loaded on first use
   bool have_w = false;
   const int lane = threadIdx.x & 31;
@@ -668,61 +639,33 @@ __global__ void __launch_bounds__(SCAN_THREADS) peel_kernel(qsft_plan plan) {
       if (fresh) list[pos] = lb;
     }
   }
-}
-
-// Per job: iteration count, cumulative peel count and the loop's stopping
-// rules (qsft/qsft.py:151, 204-205).  One block walks all jobs; when the
-// iteration loop runs as a CUDA-graph WHILE node (set_cond), thread 0 then
-// sets the loop condition: some job still running and fewer than max_iter
-// iterations done.
-__global__ void __launch_bounds__(256) iter_end_kernel(qsft_plan plan, cudaGraphConditionalHandle cond, int set_cond,
-                                                       int max_iter) {
-  __shared__ int s_iter;
-  if (threadIdx.x == 0) s_iter = 0;
+  // the block that finishes last closes the iteration (every other block's
+  // subtractions, list entries and counters are visible to it)
+  __shared__ int s_last, s_iter;
   __syncthreads();
-  if (__ldcg(plan.done_count) < plan.njobs) {
-    for (int jid = threadIdx.x; jid < plan.njobs; jid += blockDim.x) {
-      qsft_ctrl* ctl = plan.ctrl + jid;
-      const qsft_job* job = plan.jobs + jid;
-      if (ctl->done) continue;
-      const int it = ctl->iter + 1;
-      ctl->iter = it;
-      atomicMax(&s_iter, it);
-      ctl->num_peeling += ctl->n_unique;
-      if (ctl->n_multi == 0 || ctl->n_single == 0 || it >= job->max_iter || ctl->num_peeling >= job->peeling_max ||
-          ctl->err != 0) {
-        ctl->done = 1;
-        atomicAdd(plan.done_count, 1);
-      }
-      ctl->n_single = 0;
-      ctl->n_unique = 0;
-      ctl->n_cand = 0;
-      ctl->n_dirty[(it - 1) & 1] = 0;  // consumed by this iteration's scan
-    }
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_last = atomicAdd(plan.done_count + 1, 1) == (int)gridDim.x - 1;
+    s_iter = 0;
   }
   __syncthreads();
-  if (set_cond && threadIdx.x == 0)
-    cudaGraphSetConditional(cond, (__ldcg(plan.done_count) < plan.njobs && s_iter < max_iter) ? 1u : 0u);
+  if (!s_last) return;
+  __threadfence();
+  end_iteration(plan, &s_iter);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    plan.done_count[1] = 0;  // the next iteration's tickets
+    if (set_cond)
+      cudaGraphSetConditional(cond, (__ldcg(plan.done_count) < plan.njobs && s_iter < max_iter) ? 1u : 0u);
+  }
 }
 
 template <typename T>
 static int iteration(const qsft_plan* plan, int first, cudaStream_t st, cudaGraphConditionalHandle cond = 0,
                      int set_cond = 0, int max_iter = 0) {
-  if (first) {
-    const int64_t grid = (plan->total_bins + SCAN_THREADS - 1) / SCAN_THREADS;
-    if (grid > 0x7fffffffLL) return QSFT_ERR_TOO_LARGE;
-    scan_all_kernel<T><<<(unsigned)grid, SCAN_THREADS, 0, st>>>(*plan);
-  } else {
-    scan_dirty_kernel<T><<<LIST_BLOCKS, SCAN_THREADS, 0, st>>>(*plan);
-  }
+  detect_kernel<T><<<DET_BLOCKS, DEC_THREADS, 0, st>>>(*plan, first);
   QSFT_CUDA_CHECK_LAUNCH();
-  decode_kernel<T><<<DEC_BLOCKS, DEC_THREADS, 0, st>>>(*plan);
-  QSFT_CUDA_CHECK_LAUNCH();
-  record_kernel<<<LIST_BLOCKS, SCAN_THREADS, 0, st>>>(*plan);
-  QSFT_CUDA_CHECK_LAUNCH();
-  peel_kernel<T><<<LIST_BLOCKS, SCAN_THREADS, 0, st>>>(*plan);
-  QSFT_CUDA_CHECK_LAUNCH();
-  iter_end_kernel<<<1, 256, 0, st>>>(*plan, cond, set_cond, max_iter);
+  peel_kernel<T><<<LIST_BLOCKS, PEEL_THREADS, 0, st>>>(*plan, cond, set_cond, max_iter);
   QSFT_CUDA_CHECK_LAUNCH();
   return QSFT_OK;
 }
@@ -731,25 +674,22 @@ static int iteration(const qsft_plan* plan, int first, cudaStream_t st, cudaGrap
 template <typename T>
 static int add_body(const qsft_plan* plan, cudaGraph_t body, cudaGraphConditionalHandle cond, int max_iter) {
   qsft_plan pl = *plan;
-  int set = 1, mi = max_iter;
-  void* a1[] = {&pl};
-  void* a5[] = {&pl, &cond, &set, &mi};
+  int first = 0, set = 1, mi = max_iter;
+  void* a1[] = {&pl, &first};
+  void* a2[] = {&pl, &cond, &set, &mi};
   struct K {
     void* f;
-    unsigned grid, block, smem;
+    unsigned grid, block;
     void** args;
-  } ks[] = {{(void*)scan_dirty_kernel<T>, LIST_BLOCKS, SCAN_THREADS, 0, a1},
-            {(void*)decode_kernel<T>, DEC_BLOCKS, DEC_THREADS, 0, a1},
-            {(void*)record_kernel, LIST_BLOCKS, SCAN_THREADS, 0, a1},
-            {(void*)peel_kernel<T>, LIST_BLOCKS, SCAN_THREADS, 0, a1},
-            {(void*)iter_end_kernel, 1, 256, 0, a5}};
+  } ks[] = {{(void*)detect_kernel<T>, DET_BLOCKS, DEC_THREADS, a1},
+            {(void*)peel_kernel<T>, LIST_BLOCKS, PEEL_THREADS, a2}};
   cudaGraphNode_t prev = nullptr;
   for (const K& k : ks) {
     cudaKernelNodeParams kp = {};
     kp.func = k.f;
     kp.gridDim = dim3(k.grid);
     kp.blockDim = dim3(k.block);
-    kp.sharedMemBytes = k.smem;
+    kp.sharedMemBytes = 0;
     kp.kernelParams = k.args;
     cudaGraphNode_t node;
     if (cudaGraphAddKernelNode(&node, body, prev ? &prev : nullptr, prev ? 1 : 0, &kp) != cudaSuccess)
@@ -790,9 +730,9 @@ static int run_graph(const qsft_plan* plan, int max_iter, cudaStream_t st) {
 }
 
 static int check_plan(const qsft_plan* p) {
-  if (!p || p->njobs <= 0 || !p->jobs || !p->bin_prefix || !p->i8 || !p->U || !p->kbuf || !p->rho || !p->ball_best ||
+  if (!p || p->njobs <= 0 || !p->jobs || !p->bin_prefix || !p->i8 || !p->U || !p->rho || !p->ball_best ||
       !p->uniq || !p->ball_tab || !p->ball_k || !p->ball_sum || !p->ball_cnt ||
-      !p->ctrl || !p->roots || !p->bin_status || !p->bin_stamp || !p->dirty || !p->cand || !p->done_count)
+      !p->ctrl || !p->roots || !p->bin_status || !p->bin_stamp || !p->dirty || !p->done_count)
     return QSFT_ERR_ARG;
   if (p->kstride < 16 || (p->kstride & 15) || p->kstride > 2 * QSFT_MAX_N) return QSFT_ERR_ARG;
   if (p->max_q > QSFT_MAX_Q || p->max_n > QSFT_MAX_N) return QSFT_ERR_TOO_LARGE;
@@ -815,7 +755,7 @@ extern "C" int qsft_peel_init(const qsft_plan* plan, qsft_stream_t stream) {
       cudaMemsetAsync(plan->ball_sum, 0, sizeof(double) * 2 * plan->total_balls, st) != cudaSuccess ||
       cudaMemsetAsync(plan->ball_cnt, 0, sizeof(int32_t) * plan->total_balls, st) != cudaSuccess ||
       cudaMemsetAsync(plan->bin_stamp, 0, sizeof(int32_t) * plan->total_bins, st) != cudaSuccess ||
-      cudaMemsetAsync(plan->done_count, 0, sizeof(int32_t), st) != cudaSuccess)
+      cudaMemsetAsync(plan->done_count, 0, 2 * sizeof(int32_t), st) != cudaSuccess)
     return QSFT_ERR_CUDA;
   return QSFT_OK;
 }

@@ -280,10 +280,10 @@ class Batch:
         block, _, _ = self._index_block()
         sizes = [max(self.n_i8, 1), max(self.n_a, 1) * es, max(self.n_u, 1) * es, ctypes.sizeof(QsftJob) * J,
                  block.nbytes,                                                      # packed index arrays
-                 bins * 16, bins * ks, slots * 8, balls * 8, balls * 4,             # rho, kbuf, ball table, best, uniq
+                 bins * 16, slots * 8, balls * 8, balls * 4,                        # rho, ball table, best, uniq
                  balls * ks, balls * 16, balls * 4,                                 # ball k, sum, count
-                 bins, bins * 4, 2 * bins * 4, bins * 4,                            # status, stamp, dirty, cand
-                 balls * ks, balls * 16, balls * 4, (2 + 2 * J + cs * J) * 8, 4]    # outputs, metadata, done
+                 bins, bins * 4, 2 * bins * 4,                                      # status, stamp, dirty
+                 balls * ks, balls * 16, balls * 4, (2 + 2 * J + cs * J) * 8, 8]    # outputs, metadata, done
         if self.prec == QSFT_F32:
             p = QsftPlan()
             index = (ctypes.c_int64 * (3 * J + 2))()
@@ -330,7 +330,6 @@ class Batch:
         self.gwht_meta = {k: view(("meta", k)) for k in self.gwht_meta_host}
         self.roots = roots_table(dev)
         self.rho = z(self.total_bins * 2, torch.float64)
-        self.kbuf = z(self.total_bins * self.kstride, torch.uint8)
         self.ball_tab = z(self.total_slots, torch.int64)
         self.ball_best = z(self.total_balls, torch.int64)
         self.uniq = z(self.total_balls, torch.int32)
@@ -340,7 +339,6 @@ class Batch:
         self.bin_status = z(self.total_bins, torch.uint8)
         self.bin_stamp = z(self.total_bins, torch.int32)
         self.dirty = z(2 * self.total_bins, torch.int32)
-        self.cand = z(self.total_bins, torch.int32)
         self.out_k = z(self.total_balls * self.kstride, torch.uint8)
         self.out_val = z(self.total_balls * 2, torch.float64)
         self.out_cnt = z(self.total_balls, torch.int32)
@@ -368,12 +366,12 @@ class Batch:
         ptr = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
         p.jobs, p.eval_prefix, p.bin_prefix = ptr(self.jobs_dev), ptr(self.eval_prefix), ptr(self.bin_prefix)
         p.i8, p.A, p.U, p.gf_tables, p.roots = ptr(self.i8), ptr(self.A), ptr(self.U), ptr(self.gf), ptr(self.roots)
-        p.kbuf, p.rho, p.ball_tab, p.ball_best = ptr(self.kbuf), ptr(self.rho), ptr(self.ball_tab), ptr(self.ball_best)
+        p.rho, p.ball_tab, p.ball_best = ptr(self.rho), ptr(self.ball_tab), ptr(self.ball_best)
         p.uniq, p.ball_k = ptr(self.uniq), ptr(self.ball_k)
         p.ball_sum, p.ball_cnt, p.ctrl = ptr(self.ball_sum), ptr(self.ball_cnt), ptr(self.ctrl)
         p.bin_status, p.bin_stamp = ptr(self.bin_status), ptr(self.bin_stamp)
-        p.dirty, p.cand = ptr(self.dirty), ptr(self.cand)
-        self.done_count = z(1, torch.int32)
+        p.dirty = ptr(self.dirty)
+        self.done_count = z(2, torch.int32)
         p.done_count = ptr(self.done_count)
         p.tc_prefix, p.total_tc_work = ptr(self.tc_prefix), self.tc_prefix_host[-1]
         p.tc_smax, p.tc_npad, p.tc_table_bytes = self.tc_smax, self.tc_npad, self.tc_table_bytes

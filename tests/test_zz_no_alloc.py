@@ -6,7 +6,7 @@ the workspace path (qsft_peel_init/run/collect on a Batch) on the same bins,
 twice in a row since every call reuses the library's one static scratch
 array: same support, coefficients within the FP32 / FP64 tolerances of the
 other parity tests, and the same control record (no table error, the same
-iteration count and ball count).  This file sorts last so that a
+iteration count and peel count).  This file sorts last so that a
 stop-at-first-failure run has executed every other test first."""
 import ctypes
 
@@ -61,8 +61,11 @@ def test_peel_noalloc_matches_workspace_path(cuda, prec):
         ctrl = _lib.QsftCtrl.from_buffer_copy(out_ctrl.cpu().numpy().tobytes())
         assert ctrl.err == 0, f"call {call}: device table error {ctrl.err}"
         assert ctrl.done == 1 and ctrl.iter == ctrl_ws.iter, f"call {call}: {ctrl.iter} vs {ctrl_ws.iter} iterations"
-        assert ctrl.n_balls == ctrl_ws.n_balls and ctrl.num_peeling == ctrl_ws.num_peeling
+        assert ctrl.num_peeling == ctrl_ws.num_peeling
         m = int(out_total.item())
+        # ball ids handed out: one per distinct k, plus any that two threads inserting
+        # the same k at once allocated (left empty, skipped by the collection)
+        assert ctrl.n_balls >= m
         k = out_k[:m * _lib.NOALLOC_KSTRIDE].cpu().numpy().reshape(m, -1)[:, :job.n]
         v = out_val[:2 * m].cpu().numpy().reshape(m, 2)
         got = _dict(k, v[:, 0] + 1j * v[:, 1])
