@@ -143,6 +143,13 @@ typedef struct qsft_plan {
   uint8_t* bin_status;         /* [total_bins] 0 zeroton, 1 multiton, 2 singleton  */
   int32_t* bin_stamp;          /* [total_bins] last iteration that changed the bin  */
   int32_t* dirty;              /* [2 * total_bins] changed bins, by iteration parity */
+  int32_t* cand;               /* [total_bins] bins above the energy cutoff in this
+                                * iteration, job j's list at jobs[j].off_bin       */
+  /* staged copies of the candidates' columns, for the decoder: job j owns the
+   * columns [bin_prefix[j] / 8, bin_prefix[j+1] / 8) of stage_rp complex values
+   * (prec); candidates beyond that share, or jobs with R*P > stage_rp, are read
+   * from U.  NULL: no staging.                                                  */
+  void* stage;                 /* [(total_bins / 8) * stage_rp] complex             */
   int32_t* done_count;         /* [2]: [0] jobs whose loop has ended (the peeling
                                 * kernels exit at once when it reaches njobs);
                                 * [1] blocks of the running peel launch that have
@@ -158,7 +165,7 @@ typedef struct qsft_plan {
   int32_t tc_entry_bytes;      /* shared-memory table bytes per support entry:
                                 * q*q*4 when every job has the same q in {2, 4}
                                 * (pair table), else max_q*8                        */
-  int32_t pad2_;
+  int32_t stage_rp;            /* column length of `stage` (1..64; min(max R*P, 64)) */
   int32_t* status;             /* [1] device word, 0 = ok, else a qsft_status       */
   /* coset-factored tensor-core evaluation (qsft_eval_cosets_gemm); the gm_*
    * sizes and counts are filled in by qsft_gemm_layout                         */
@@ -302,9 +309,9 @@ int qsft_peel_init(const qsft_plan* plan, qsft_stream_t stream);
  * function of the bin's unchanged values, so the outcome is the same.
  */
 int qsft_peel_iteration(const qsft_plan* plan, int first, qsft_stream_t stream);
-/* kernels one peeling iteration launches (detect: zeroton test, decoding and
- * recording of singletons; peel: subtraction and the iteration's end) */
-#define QSFT_PEEL_LAUNCHES_PER_ITER 2
+/* kernels one peeling iteration launches (scan: zeroton test; decode: decoding
+ * and recording of singletons; peel: subtraction and the iteration's end) */
+#define QSFT_PEEL_LAUNCHES_PER_ITER 3
 /*
  * Up to max_iter iterations.  Issued eagerly, all max_iter are launched
  * (iterations of finished jobs are no-ops).  Inside a stream capture,
@@ -356,7 +363,7 @@ int qsft_rs_decode(int q, int s, int t, int n, const int32_t* gf_tables, const u
  * applications that own every buffer (a fixed memory budget or a pool of
  * their own) and hand a library only its inputs and outputs.  All scratch
  * (hash tables, result store, lists, roots table, control record) lives in a
- * statically sized device array inside the library (about 1.8 MB, held by
+ * statically sized device array inside the library (about 1.9 MB, held by
  * every GPU that loads the library until the process exits), so the call
  * allocates nothing.  `job` is a host record (offsets off_M/off_D into i8,
  * off_U into U; qsft_workspace_layout's fields are filled in by the call); U

@@ -23,7 +23,7 @@ TC_TILE_M = 128
 NOALLOC_MAX_BINS = 16384   # QSFT_NOALLOC_MAX_BINS
 NOALLOC_KSTRIDE = 32       # QSFT_NOALLOC_KSTRIDE
 TC_SUB_N = 128
-PEEL_LAUNCHES_PER_ITER = 2   # QSFT_PEEL_LAUNCHES_PER_ITER
+PEEL_LAUNCHES_PER_ITER = 3   # QSFT_PEEL_LAUNCHES_PER_ITER
 
 # exported symbols, in header order
 SYMBOLS = [
@@ -79,10 +79,10 @@ class QsftPlan(ctypes.Structure):
         ("gf_tables", _P), ("roots", _P),
         ("rho", _P), ("ball_tab", _P), ("ball_best", _P), ("uniq", _P),
         ("ball_k", _P), ("ball_sum", _P), ("ball_cnt", _P), ("ctrl", _P),
-        ("bin_status", _P), ("bin_stamp", _P), ("dirty", _P), ("done_count", _P),
+        ("bin_status", _P), ("bin_stamp", _P), ("dirty", _P), ("cand", _P), ("stage", _P), ("done_count", _P),
         ("tc_prefix", _P), ("total_tc_work", ctypes.c_int64), ("tc_smax", ctypes.c_int32),
         ("tc_npad", ctypes.c_int32), ("min_q", ctypes.c_int32), ("tc_table_bytes", ctypes.c_int32),
-        ("tc_entry_bytes", ctypes.c_int32), ("pad2_", ctypes.c_int32), ("status", _P),
+        ("tc_entry_bytes", ctypes.c_int32), ("stage_rp", ctypes.c_int32), ("status", _P),
         ("gm_ws", _P), ("gm_index", _P), ("total_gm_work", ctypes.c_int64), ("total_gm_prep", ctypes.c_int64),
         ("gm_ws_bytes", ctypes.c_int64), ("gm_mt", ctypes.c_int32), ("gm_kps", ctypes.c_int32),
         ("gm_nw", ctypes.c_int32), ("gm_npmax", ctypes.c_int32), ("gm_jt_bytes", ctypes.c_int32),

@@ -48,7 +48,8 @@ constexpr size_t OFF_BALLCNT = al(OFF_BALLSUM + MAX_BALLS * 2 * sizeof(double));
 constexpr size_t OFF_STATUS = al(OFF_BALLCNT + MAX_BALLS * sizeof(int32_t));
 constexpr size_t OFF_STAMP = al(OFF_STATUS + MAX_BINS);
 constexpr size_t OFF_DIRTY = al(OFF_STAMP + MAX_BINS * sizeof(int32_t));
-constexpr size_t TOTAL = al(OFF_DIRTY + 2 * MAX_BINS * sizeof(int32_t));
+constexpr size_t OFF_CAND = al(OFF_DIRTY + 2 * MAX_BINS * sizeof(int32_t));
+constexpr size_t TOTAL = al(OFF_CAND + MAX_BINS * sizeof(int32_t));
 
 // the scratch: held by every GPU that loads the library, shared by every call
 static __device__ __align__(256) unsigned char g_scratch[TOTAL];
@@ -144,6 +145,8 @@ extern "C" int qsft_peel_noalloc(int prec, const qsft_job* job_in, const int8_t*
   p.bin_status = base + OFF_STATUS;
   p.bin_stamp = reinterpret_cast<int32_t*>(base + OFF_STAMP);
   p.dirty = reinterpret_cast<int32_t*>(base + OFF_DIRTY);
+  p.cand = reinterpret_cast<int32_t*>(base + OFF_CAND);
+  p.stage = nullptr;  // no staging copies: the decoder reads the candidates' columns from U
   p.done_count = reinterpret_cast<int32_t*>(base + OFF_DONE);
 
   // qsft_peel_init zeroes everything that must start at zero (control record,

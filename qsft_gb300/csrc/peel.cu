@@ -1,27 +1,28 @@
 // Singleton detection and peeling: QSFT.transform's while-loop
 // (qsft/qsft.py:151-255) for a batch of transforms.
 //
-// One iteration = two launches:
-//   detect   a warp takes 32 bins at a time (the first iteration: every bin,
-//            consecutive bins of a group, coalesced; later ones: the bins the
-//            previous subtractions changed -- the others keep their class, a
-//            function of their unchanged values).  Lane per bin: the zeroton
-//            test ||col||^2 > cutoff*len (qsft/qsft.py:164); the warp's
-//            candidates are then decoded four at a time by groups of 8 lanes
-//            while their columns are still in L2: channel decoding of k
+// One iteration = three launches:
+//   scan     a warp takes 32 bins at a time, a lane per bin (the first
+//            iteration: every bin, consecutive bins of a group -- coalesced;
+//            later ones: the bins the previous subtractions changed, the
+//            others keeping their class, a function of their unchanged
+//            values): the zeroton test ||col||^2 > cutoff*len
+//            (qsft/qsft.py:164).  Bins above it are queued and their columns
+//            copied, while still in L2, into a compact staging buffer.
+//   decode   a group of 8 lanes per queued bin: channel decoding of k
 //            (noiseless qsft/reconstruct.py:12-31 or NSO "nso1" :100-113),
 //            optional Reed-Solomon source decoding (:34-51), projection
 //            rho = <omega^(Dk), col>/len and residual energy, bin-match test
-//            (qsft/qsft.py:174-190).  Each singleton is recorded at once:
-//            it finds (or creates) the ball of its k in a persistent hash
-//            table, adds rho to the ball's running sum (the `result` list and
-//            its mean, :217, 247-255) and marks the ball detected in this
+//            (qsft/qsft.py:174-190).  Each singleton is recorded at once: it
+//            finds (or creates) the ball of its k in a persistent hash table,
+//            adds rho to the ball's running sum (the `result` list and its
+//            mean, :217, 247-255) and marks the ball detected in this
 //            iteration keeping the largest (group, bin) -- the reference's
 //            dict order, `ball_values` (:209-216).
 //   peel     per (detected ball, group l) -- a thread, or 8 for short lists:
 //            subtract rho * omega^(D_l k) from bin M_l^T k (mod q) of group l
 //            (qsft/qsft.py:223-241) and queue the changed bin for the next
-//            detect.  The block that finishes last closes the iteration for
+//            scan.  The block that finishes last closes the iteration for
 //            every job: iteration count, cumulative peel count and the loop's
 //            stopping rules (qsft/qsft.py:151, 204-205).
 //
@@ -80,9 +81,9 @@ __device__ __forceinline__ double warp_sum(double v) {
 // ||col||^2 with the FP64 recomputation band of the FP32 path
 template <typename T>
 __device__ __forceinline__ double col_energy(const c2<T>* col, int RP, int B, double thr) {
-  // the loads of 16 rows are issued before their sum (in row order) is taken:
-  // a lane keeps 16 independent loads in flight instead of a few
-  constexpr int BATCH = 16;
+  // the loads of 16 rows (8 in FP64) are issued before their sum (in row
+  // order) is taken: a lane keeps that many independent loads in flight
+  constexpr int BATCH = sizeof(T) == 4 ? 16 : 8;
   T e = 0;
   for (int r0 = 0; r0 < RP; r0 += BATCH) {
     c2<T> v[BATCH];
@@ -170,12 +171,6 @@ __device__ __forceinline__ V group_sum_g(V v, unsigned mask, int g) {
   return v;
 }
 
-// n-th (from 0) set bit of m, n < popc(m)
-__device__ __forceinline__ int nth_set(unsigned m, int n) {
-  for (int i = 0; i < n; ++i) m &= m - 1;
-  return __ffs(m) - 1;
-}
-
 // ---------------------------------------------------------------- record
 // One singleton (k in the 16-byte aligned row kr, coefficient rho) of bin
 // `local`: find (or create) the ball of its k in the job's persistent table
@@ -238,12 +233,86 @@ __device__ __forceinline__ int record_one(const qsft_plan& plan, const qsft_job*
   return bid;
 }
 
-// ---------------------------------------------------------------- detect
-constexpr int DET_BLOCKS = 152 * 5;   // resident at once (5 blocks of 128 threads per SM)
+// ---------------------------------------------------------------- scan
+// The staged copy of candidate `pos`'s column of job `jid`: job j owns staging
+// columns [bin_prefix[j] / 8, bin_prefix[j+1] / 8), of stage_rp entries each.
+// nullptr (the decoder then reads the column from U): no staging buffer, a
+// column longer than stage_rp, or more candidates than the job's share.
+template <typename T>
+__device__ __forceinline__ c2<T>* stage_col(const qsft_plan& plan, int jid, int pos, int RP) {
+  if (!plan.stage || RP > plan.stage_rp) return nullptr;
+  const int64_t s0 = __ldg(plan.bin_prefix + jid) / 8, s1 = __ldg(plan.bin_prefix + jid + 1) / 8;
+  if (pos >= s1 - s0) return nullptr;
+  return reinterpret_cast<c2<T>*>(plan.stage) + (s0 + pos) * plan.stage_rp;
+}
+
+// A warp takes 32 bins at a time, a lane per bin: the first iteration every
+// bin (consecutive bins of a group: coalesced rows), later ones the bins the
+// previous iteration's subtractions changed.  Each bin's class is reset (the
+// multiton count kept up to date); a bin above the energy cutoff is queued in
+// the job's candidate list, and the warp copies its column into the staging
+// buffer at once -- the values are still in L2 -- so that the decoder reads
+// one contiguous column instead of RP scattered sectors from HBM.
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_BLOCKS = 152 * 8;
 
 template <typename T>
-// FP32: 5 blocks per SM (up to 102 registers: no spill)
-__global__ void __launch_bounds__(DEC_THREADS, sizeof(T) == 4 ? 5 : 4) detect_kernel(qsft_plan plan, int first) {
+__global__ void __launch_bounds__(SCAN_THREADS, sizeof(T) == 4 ? 4 : 3) scan_kernel(qsft_plan plan, int first) {
+  if (__ldcg(plan.done_count) >= plan.njobs) return;  // every job has left the loop
+  const int lane = threadIdx.x & 31;
+  const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+  int64_t chunk0 = 0;  // 32-bin chunks of all jobs are dealt round-robin to the warps
+  for (int jid = 0; jid < plan.njobs; ++jid) {
+    qsft_ctrl* ctl = plan.ctrl + jid;
+    if (ctl->done) continue;
+    const qsft_job* __restrict__ job = plan.jobs + jid;
+    const int B = job->B, RP = job->R * job->P;
+    const int parity = ctl->iter & 1;   // the dirty list the peel of iteration `iter` wrote
+    const int cnt = first ? job->C * B : ctl->n_dirty[parity];
+    const int nch = (cnt + 31) >> 5;
+    const int start = (int)(((int64_t)gw - chunk0) % nw + nw) % nw;
+    chunk0 += nch;
+    if (start >= nch) continue;
+    const double thr = job->cutoff * RP;
+    const int32_t* list = plan.dirty + (int64_t)parity * plan.total_bins + job->off_bin;
+    const c2<T>* U = reinterpret_cast<const c2<T>*>(plan.U) + job->off_U;
+    for (int ch = start; ch < nch; ch += nw) {   // uniform over the warp
+      const int i = ch * 32 + lane;
+      bool is_cand = false;
+      int local = 0;
+      if (i < cnt) {
+        local = first ? i : list[i];
+        const int64_t gb = job->off_bin + local;
+        if (!first && plan.bin_status[gb] == 1) atomicSub(&ctl->n_multi, 1);
+        plan.bin_status[gb] = 0;
+        const int c = local / B, jb = local - (local / B) * B;
+        is_cand = col_energy<T>(U + (int64_t)c * RP * B + jb, RP, B, thr) > thr;
+      }
+      const int pos = warp_append(is_cand, jid, &ctl->n_cand);
+      if (is_cand) plan.cand[job->off_bin + pos] = local;
+      for (unsigned m = __ballot_sync(0xffffffffu, is_cand); m; m &= m - 1) {
+        const int src = __ffs(m) - 1;
+        const int p = __shfl_sync(0xffffffffu, pos, src);
+        const int lc = __shfl_sync(0xffffffffu, local, src);
+        c2<T>* dst = stage_col<T>(plan, jid, p, RP);
+        if (dst) {
+          const c2<T>* col = U + (int64_t)(lc / B) * RP * B + (lc - (lc / B) * B);
+          for (int r = lane; r < RP; r += 32) dst[r] = col[(int64_t)r * B];
+        }
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------- decode
+// Groups of DEC_G lanes take the candidates of the job's list; each singleton
+// is recorded at once (record_one) and the ball's first detection of the
+// iteration appended to the iteration's list.
+constexpr int DEC_BLOCKS = 152 * 5;   // resident at once (5 blocks of 128 threads per SM)
+
+template <typename T>
+// FP32: 5 blocks per SM (up to 102 registers)
+__global__ void __launch_bounds__(DEC_THREADS, sizeof(T) == 4 ? 5 : 4) decode_kernel(qsft_plan plan) {
   if (__ldcg(plan.done_count) >= plan.njobs) return;  // every job has left the loop
   __shared__ float2 s_w[33 * 32];                            // roots, FP32
   __shared__ c2<T> s_col[DEC_BINS][DEC_STAGE_RP];
@@ -259,224 +328,206 @@ __global__ void __launch_bounds__(DEC_THREADS, sizeof(T) == 4 ? 5 : 4) detect_ke
   const int ks = plan.kstride;
   c2<T>* sc = s_col[slot];
   uint8_t* kl = s_k[slot];
-  int64_t chunk0 = 0;  // 32-bin chunks of all jobs are dealt round-robin to the warps
+  int64_t chunk0 = 0;
   for (int jid = 0; jid < plan.njobs; ++jid) {
     qsft_ctrl* ctl = plan.ctrl + jid;
     if (ctl->done) continue;
-    const qsft_job* __restrict__ job = plan.jobs + jid;
-    const int q = job->q, n = job->n, b = job->b, B = job->B, P = job->P, R = job->R;
-    const int RP = R * P, nsym = P - 1;
-    const int parity = ctl->iter & 1;   // the dirty list the peel of iteration `iter` wrote
-    const int cnt = first ? job->C * B : ctl->n_dirty[parity];
-    const int nch = (cnt + 31) >> 5;
+    const int cnt = ctl->n_cand;
+    const int nch = (cnt + DEC_CPW - 1) / DEC_CPW;
     const int start = (int)(((int64_t)gw - chunk0) % nw + nw) % nw;
     chunk0 += nch;
     if (start >= nch) continue;
+    const qsft_job* __restrict__ job = plan.jobs + jid;
+    const int q = job->q, n = job->n, b = job->b, B = job->B, P = job->P, R = job->R;
+    const int RP = R * P, nsym = P - 1;
     const double thr = job->cutoff * RP;
     const bool staged = RP <= DEC_STAGE_RP;
     const bool words_ok = (n & 3) == 0 && ((job->off_D & 3) == 0);
     const float2* wq = s_w + q * 32;
     uint8_t* syms = job->src == QSFT_SRC_CODED ? s_sym[slot] : kl;
     const long long iter = (long long)ctl->iter + 1;
-    const int32_t* list = plan.dirty + (int64_t)parity * plan.total_bins + job->off_bin;
     for (int ch = start; ch < nch; ch += nw) {   // uniform over the warp: every lane runs every sync
-      // ---- zeroton test, lane per bin
-      const int i = ch * 32 + lane;
-      bool is_cand = false;
-      int mylocal = 0;
-      if (i < cnt) {
-        mylocal = first ? i : list[i];
-        const int64_t gbl = job->off_bin + mylocal;
-        if (!first && plan.bin_status[gbl] == 1) atomicSub(&ctl->n_multi, 1);
-        plan.bin_status[gbl] = 0;
-        const int cc = mylocal / B, jj = mylocal - (mylocal / B) * B;
-        const c2<T>* cl = reinterpret_cast<const c2<T>*>(plan.U) + job->off_U + (int64_t)cc * RP * B + jj;
-        is_cand = col_energy<T>(cl, RP, B, thr) > thr;
-      }
-      const unsigned cmask = __ballot_sync(0xffffffffu, is_cand);
-      const int ncand = __popc(cmask);
-      if (lane == 0 && ncand) atomicAdd(&ctl->n_cand, ncand);
-      __syncwarp();  // the class resets above are ordered before the decode's writes
-      // ---- the candidates, DEC_CPW at a time
-      for (int r0 = 0; r0 < ncand; r0 += DEC_CPW) {
-        const int mine = r0 + lane / DEC_G;
-        const bool active = mine < ncand;
-        const int src_lane = active ? nth_set(cmask, mine) : 0;
-        const int local = __shfl_sync(0xffffffffu, mylocal, src_lane);
-        const int c = local / B, jb = local - (local / B) * B;
-        const int64_t gb = job->off_bin + local;
-        const c2<T>* col = reinterpret_cast<const c2<T>*>(plan.U) + job->off_U + (int64_t)c * RP * B + jb;
-        if (staged && active)
+      const int u = ch * DEC_CPW + lane / DEC_G;
+      const bool active = u < cnt;
+      const int local = active ? plan.cand[job->off_bin + u] : 0;
+      const int c = local / B, jb = local - (local / B) * B;
+      const int64_t gb = job->off_bin + local;
+      const c2<T>* col = reinterpret_cast<const c2<T>*>(plan.U) + job->off_U + (int64_t)c * RP * B + jb;
+      const c2<T>* stg = active ? stage_col<T>(plan, jid, u, RP) : nullptr;
+      if (staged && active) {
+        if (stg)
+          for (int r = gi; r < RP; r += DEC_G) sc[r] = stg[r];
+        else
           for (int r = gi; r < RP; r += DEC_G) sc[r] = col[(int64_t)r * B];
-        __syncwarp();
-        auto V = [&](int r) -> c2<T> { return staged ? sc[r] : col[(int64_t)r * B]; };
-        // ---- channel decoding, symbols dealt over the group
-        if (active) {
-          if (job->chan == QSFT_CHAN_IDENTITY) {
-            const c2<T> v0 = V(0);
-            const T a0 = atan2(v0.y, v0.x);
-            for (int i = 1 + gi; i < RP && i <= nsym; i += DEC_G) {
-              const c2<T> vi = V(i);
-              const T ai = atan2(vi.y, vi.x);
-              double a = (double)((T)q * (ai - a0) / (T)6.283185307179586);
-              if (sizeof(T) == 4 && fabs(a - floor(a) - 0.5) < 1e-3)
-                a = (double)q * (atan2((double)vi.y, (double)vi.x) - atan2((double)v0.y, (double)v0.x)) /
-                    6.283185307179586;
-              long long m = (long long)rint(a);  // round half to even, like np.round
-              m %= q;
-              if (m < 0) m += q;
-              syms[i - 1] = (uint8_t)m;
+      }
+      __syncwarp();
+      auto V = [&](int r) -> c2<T> { return staged ? sc[r] : col[(int64_t)r * B]; };
+      // ---- channel decoding, symbols dealt over the group
+      if (active) {
+        if (job->chan == QSFT_CHAN_IDENTITY) {
+          const c2<T> v0 = V(0);
+          const T a0 = atan2(v0.y, v0.x);
+          for (int i = 1 + gi; i < RP && i <= nsym; i += DEC_G) {
+            const c2<T> vi = V(i);
+            const T ai = atan2(vi.y, vi.x);
+            double a = (double)((T)q * (ai - a0) / (T)6.283185307179586);
+            if (sizeof(T) == 4 && fabs(a - floor(a) - 0.5) < 1e-3)
+              a = (double)q * (atan2((double)vi.y, (double)vi.x) - atan2((double)v0.y, (double)v0.x)) /
+                  6.283185307179586;
+            long long m = (long long)rint(a);  // round half to even, like np.round
+            m %= q;
+            if (m < 0) m += q;
+            syms[i - 1] = (uint8_t)m;
+          }
+        } else {
+          for (int i = 1 + gi; i <= nsym; i += DEC_G) {
+            T zr = 0, zi = 0;
+            for (int r = 0; r < R; ++r) {
+              const c2<T> u0 = V(r * P), ui = V(r * P + i);
+              zr += u0.x * ui.x + u0.y * ui.y;
+              zi += u0.y * ui.x - u0.x * ui.y;
             }
-          } else {
-            for (int i = 1 + gi; i <= nsym; i += DEC_G) {
-              T zr = 0, zi = 0;
+            if (sizeof(T) == 4) {
+              float ang = atan2f((float)zi, (float)zr);
+              if (ang < 0.f) ang += 6.28318530717958647f;
+              const float tq = ang * (float)q * 0.15915494309189535f;
+              if (fabsf(tq - floorf(tq) - 0.5f) >= 1e-3f) {
+                // away from a tie the nearest of 2 pi m / q, m = 0..q, is floor(tq + 1/2)
+                syms[i - 1] = (uint8_t)(((int)floorf(tq + 0.5f)) % q);
+                continue;
+              }
+              double dzr = 0, dzi = 0;  // near a rounding boundary: recompute in FP64
               for (int r = 0; r < R; ++r) {
-                const c2<T> u0 = V(r * P), ui = V(r * P + i);
-                zr += u0.x * ui.x + u0.y * ui.y;
-                zi += u0.y * ui.x - u0.x * ui.y;
+                const double2 u0 = to_d2(V(r * P)), ui = to_d2(V(r * P + i));
+                dzr += u0.x * ui.x + u0.y * ui.y;
+                dzi += u0.y * ui.x - u0.x * ui.y;
               }
-              if (sizeof(T) == 4) {
-                float ang = atan2f((float)zi, (float)zr);
-                if (ang < 0.f) ang += 6.28318530717958647f;
-                const float tq = ang * (float)q * 0.15915494309189535f;
-                if (fabsf(tq - floorf(tq) - 0.5f) >= 1e-3f) {
-                  // away from a tie the nearest of 2 pi m / q, m = 0..q, is floor(tq + 1/2)
-                  syms[i - 1] = (uint8_t)(((int)floorf(tq + 0.5f)) % q);
-                  continue;
-                }
-                double dzr = 0, dzi = 0;  // near a rounding boundary: recompute in FP64
-                for (int r = 0; r < R; ++r) {
-                  const double2 u0 = to_d2(V(r * P)), ui = to_d2(V(r * P + i));
-                  dzr += u0.x * ui.x + u0.y * ui.y;
-                  dzi += u0.y * ui.x - u0.x * ui.y;
-                }
-                double ang64 = atan2(dzi, dzr);
-                if (ang64 < 0) ang64 += 6.283185307179586;
-                syms[i - 1] = (uint8_t)nearest_root(ang64, q);
-              } else {
-                double ang = (double)atan2(zi, zr);
-                if (ang < 0) ang += 6.283185307179586;
-                syms[i - 1] = (uint8_t)nearest_root(ang, q);
-              }
+              double ang64 = atan2(dzi, dzr);
+              if (ang64 < 0) ang64 += 6.283185307179586;
+              syms[i - 1] = (uint8_t)nearest_root(ang64, q);
+            } else {
+              double ang = (double)atan2(zi, zr);
+              if (ang < 0) ang += 6.283185307179586;
+              syms[i - 1] = (uint8_t)nearest_root(ang, q);
             }
           }
         }
-        __syncwarp();
-        // ---- source decoding
-        const bool coded = job->src == QSFT_SRC_CODED;
-        if (coded && active && gi == 0) {
-          const GFt g = make_gf(plan.gf_tables + job->rs_gf_off, q, job->rs_s);
-          rs_decode(g, q, job->rs_s, job->rs_t, n, syms, kl, kl + n);
+      }
+      __syncwarp();
+      // ---- source decoding
+      const bool coded = job->src == QSFT_SRC_CODED;
+      if (coded && active && gi == 0) {
+        const GFt g = make_gf(plan.gf_tables + job->rs_gf_off, q, job->rs_s);
+        rs_decode(g, q, job->rs_s, job->rs_t, n, syms, kl, kl + n);
+      }
+      __syncwarp();
+      for (int i = (coded ? 2 * n : n) + gi; i < ks; i += DEC_G) kl[i] = 0;
+      __syncwarp();
+      // ---- projection rho = <omega^(Dk), col> / RP and residual energy, rows
+      //      dealt over the group: FP32 for FP32 plans (FP64 within 1% of the
+      //      threshold), FP64 for FP64 plans
+      const int8_t* Dc = plan.i8 + job->off_D + (int64_t)c * RP * n;
+      auto project64 = [&](double2& rho_out, double& res_out) {
+        double ar = 0, ai = 0;
+        for (int r = gi; r < RP; r += DEC_G) {
+          const double2 w = root(plan.roots, q, row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q));
+          const double2 v = to_d2(V(r));
+          ar += w.x * v.x + w.y * v.y;
+          ai += w.x * v.y - w.y * v.x;
         }
-        __syncwarp();
-        for (int i = (coded ? 2 * n : n) + gi; i < ks; i += DEC_G) kl[i] = 0;
-        __syncwarp();
-        // ---- projection rho = <omega^(Dk), col> / RP and residual energy, rows
-        //      dealt over the group: FP32 for FP32 plans (FP64 within 1% of the
-        //      threshold), FP64 for FP64 plans
-        const int8_t* Dc = plan.i8 + job->off_D + (int64_t)c * RP * n;
-        auto project64 = [&](double2& rho_out, double& res_out) {
-          double ar = 0, ai = 0;
-          for (int r = gi; r < RP; r += DEC_G) {
-            const double2 w = root(plan.roots, q, row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q));
-            const double2 v = to_d2(V(r));
-            ar += w.x * v.x + w.y * v.y;
-            ai += w.x * v.y - w.y * v.x;
-          }
-          ar = group_sum(ar, gmask);
-          ai = group_sum(ai, gmask);
-          const double2 rh = make_double2(ar / RP, ai / RP);
-          double rs = 0;
-          for (int r = gi; r < RP; r += DEC_G) {
-            const double2 w = root(plan.roots, q, row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q));
-            const double2 v = to_d2(V(r));
-            const double dx = v.x - (rh.x * w.x - rh.y * w.y);
-            const double dy = v.y - (rh.x * w.y + rh.y * w.x);
-            rs += dx * dx + dy * dy;
-          }
-          rho_out = rh;
-          res_out = group_sum(rs, gmask);
-        };
-        double2 rho = make_double2(0.0, 0.0);
-        double res = 0.0;
-        if (sizeof(T) == 4) {
-          int ph[(DEC_STAGE_RP + DEC_G - 1) / DEC_G];
-          float ar = 0.f, ai = 0.f;
-  #pragma unroll
-          for (int k = 0; k < (DEC_STAGE_RP + DEC_G - 1) / DEC_G; ++k) {
-            const int r = gi + k * DEC_G;
-            ph[k] = 0;
-            if (r < RP) {
-              ph[k] = row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q);
-              const float2 w = wq[ph[k]];
-              const c2<T> v = V(r);
-              ar += w.x * (float)v.x + w.y * (float)v.y;
-              ai += w.x * (float)v.y - w.y * (float)v.x;
-            }
-          }
-          for (int r = gi + DEC_STAGE_RP; r < RP; r += DEC_G) {  // rows past the register-held phases
-            const float2 w = wq[row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q)];
+        ar = group_sum(ar, gmask);
+        ai = group_sum(ai, gmask);
+        const double2 rh = make_double2(ar / RP, ai / RP);
+        double rs = 0;
+        for (int r = gi; r < RP; r += DEC_G) {
+          const double2 w = root(plan.roots, q, row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q));
+          const double2 v = to_d2(V(r));
+          const double dx = v.x - (rh.x * w.x - rh.y * w.y);
+          const double dy = v.y - (rh.x * w.y + rh.y * w.x);
+          rs += dx * dx + dy * dy;
+        }
+        rho_out = rh;
+        res_out = group_sum(rs, gmask);
+      };
+      double2 rho = make_double2(0.0, 0.0);
+      double res = 0.0;
+      if (sizeof(T) == 4) {
+        int ph[(DEC_STAGE_RP + DEC_G - 1) / DEC_G];
+        float ar = 0.f, ai = 0.f;
+#pragma unroll
+        for (int k = 0; k < (DEC_STAGE_RP + DEC_G - 1) / DEC_G; ++k) {
+          const int r = gi + k * DEC_G;
+          ph[k] = 0;
+          if (r < RP) {
+            ph[k] = row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q);
+            const float2 w = wq[ph[k]];
             const c2<T> v = V(r);
             ar += w.x * (float)v.x + w.y * (float)v.y;
             ai += w.x * (float)v.y - w.y * (float)v.x;
           }
-          ar = group_sum(ar, gmask) / (float)RP;
-          ai = group_sum(ai, gmask) / (float)RP;
-          float rs = 0.f;
-  #pragma unroll
-          for (int k = 0; k < (DEC_STAGE_RP + DEC_G - 1) / DEC_G; ++k) {
-            const int r = gi + k * DEC_G;
-            if (r < RP) {
-              const float2 w = wq[ph[k]];
-              const c2<T> v = V(r);
-              const float dx = (float)v.x - (ar * w.x - ai * w.y);
-              const float dy = (float)v.y - (ar * w.y + ai * w.x);
-              rs += dx * dx + dy * dy;
-            }
-          }
-          for (int r = gi + DEC_STAGE_RP; r < RP; r += DEC_G) {
-            const float2 w = wq[row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q)];
+        }
+        for (int r = gi + DEC_STAGE_RP; r < RP; r += DEC_G) {  // rows past the register-held phases
+          const float2 w = wq[row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q)];
+          const c2<T> v = V(r);
+          ar += w.x * (float)v.x + w.y * (float)v.y;
+          ai += w.x * (float)v.y - w.y * (float)v.x;
+        }
+        ar = group_sum(ar, gmask) / (float)RP;
+        ai = group_sum(ai, gmask) / (float)RP;
+        float rs = 0.f;
+#pragma unroll
+        for (int k = 0; k < (DEC_STAGE_RP + DEC_G - 1) / DEC_G; ++k) {
+          const int r = gi + k * DEC_G;
+          if (r < RP) {
+            const float2 w = wq[ph[k]];
             const c2<T> v = V(r);
             const float dx = (float)v.x - (ar * w.x - ai * w.y);
             const float dy = (float)v.y - (ar * w.y + ai * w.x);
             rs += dx * dx + dy * dy;
           }
-          rs = group_sum(rs, gmask);
-          rho = make_double2(ar, ai);
-          res = rs;
-          if (fabsf(rs - (float)thr) <= 1e-2f * (float)thr) project64(rho, res);  // group-uniform
-        } else {
-          project64(rho, res);
         }
-        // ---- bin match: digit t of M_c^T k equals digit t of j (MSB first), digits over the group
-        bool ok = true;
-        {
-          const int8_t* Mc = plan.i8 + job->off_M + (int64_t)c * n * b;
-          for (int t = gi; t < b; t += DEC_G) {
-            int jr = jb;
-            for (int tt = b - 1; tt > t; --tt) jr /= q;
-            int dg = 0;
-            for (int i = 0; i < n; ++i) dg += (int)Mc[i * b + t] * (int)kl[i];
-            ok &= (dg % q) == (jr % q);
-          }
+        for (int r = gi + DEC_STAGE_RP; r < RP; r += DEC_G) {
+          const float2 w = wq[row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q)];
+          const c2<T> v = V(r);
+          const float dx = (float)v.x - (ar * w.x - ai * w.y);
+          const float dy = (float)v.y - (ar * w.y + ai * w.x);
+          rs += dx * dx + dy * dy;
         }
-        const bool match = (__ballot_sync(0xffffffffu, !ok) & gmask) == 0;
-        const bool single = match && !(res > thr);
-        bool firstb = false;
-        int bid = -1;
-        if (active && gi == 0) {
-          plan.bin_status[gb] = single ? 2 : 1;
-          if (single) {
-            plan.rho[2 * gb] = rho.x;   // the peel reads the coefficient of the ball's last bin
-            plan.rho[2 * gb + 1] = rho.y;
-            bid = record_one(plan, job, ctl, kl, local, rho, iter, ks, firstb);
-          }
-          atomicAdd(single ? &ctl->n_single : &ctl->n_multi, 1);
-        }
-        const int pos = warp_append(firstb, jid, &ctl->n_unique);   // the iteration's list of balls
-        if (firstb) plan.uniq[job->off_ball + pos] = bid;
-        __syncwarp();  // the slot's buffers are reused by the next bin
+        rs = group_sum(rs, gmask);
+        rho = make_double2(ar, ai);
+        res = rs;
+        if (fabsf(rs - (float)thr) <= 1e-2f * (float)thr) project64(rho, res);  // group-uniform
+      } else {
+        project64(rho, res);
       }
+      // ---- bin match: digit t of M_c^T k equals digit t of j (MSB first), digits over the group
+      bool ok = true;
+      {
+        const int8_t* Mc = plan.i8 + job->off_M + (int64_t)c * n * b;
+        for (int t = gi; t < b; t += DEC_G) {
+          int jr = jb;
+          for (int tt = b - 1; tt > t; --tt) jr /= q;
+          int dg = 0;
+          for (int i = 0; i < n; ++i) dg += (int)Mc[i * b + t] * (int)kl[i];
+          ok &= (dg % q) == (jr % q);
+        }
+      }
+      const bool match = (__ballot_sync(0xffffffffu, !ok) & gmask) == 0;
+      const bool single = match && !(res > thr);
+      bool firstb = false;
+      int bid = -1;
+      if (active && gi == 0) {
+        plan.bin_status[gb] = single ? 2 : 1;
+        if (single) {
+          plan.rho[2 * gb] = rho.x;   // the peel reads the coefficient of the ball's last bin
+          plan.rho[2 * gb + 1] = rho.y;
+          bid = record_one(plan, job, ctl, kl, local, rho, iter, ks, firstb);
+        }
+        atomicAdd(single ? &ctl->n_single : &ctl->n_multi, 1);
+      }
+      const int pos = warp_append(firstb, jid, &ctl->n_unique);   // the iteration's list of balls
+      if (firstb) plan.uniq[job->off_ball + pos] = bid;
+      __syncwarp();  // the slot's buffers are reused by the next bin
     }
   }
 }
@@ -503,7 +554,7 @@ __device__ __forceinline__ void end_iteration(const qsft_plan& plan, int* s_iter
     ctl->n_single = 0;
     ctl->n_unique = 0;
     ctl->n_cand = 0;
-    ctl->n_dirty[(it - 1) & 1] = 0;  // consumed by this iteration's detect
+    ctl->n_dirty[(it - 1) & 1] = 0;  // consumed by this iteration's scan
   }
 }
 
@@ -663,7 +714,9 @@ __global__ void __launch_bounds__(PEEL_THREADS) peel_kernel(qsft_plan plan, cuda
 template <typename T>
 static int iteration(const qsft_plan* plan, int first, cudaStream_t st, cudaGraphConditionalHandle cond = 0,
                      int set_cond = 0, int max_iter = 0) {
-  detect_kernel<T><<<DET_BLOCKS, DEC_THREADS, 0, st>>>(*plan, first);
+  scan_kernel<T><<<SCAN_BLOCKS, SCAN_THREADS, 0, st>>>(*plan, first);
+  QSFT_CUDA_CHECK_LAUNCH();
+  decode_kernel<T><<<DEC_BLOCKS, DEC_THREADS, 0, st>>>(*plan);
   QSFT_CUDA_CHECK_LAUNCH();
   peel_kernel<T><<<LIST_BLOCKS, PEEL_THREADS, 0, st>>>(*plan, cond, set_cond, max_iter);
   QSFT_CUDA_CHECK_LAUNCH();
@@ -675,13 +728,15 @@ template <typename T>
 static int add_body(const qsft_plan* plan, cudaGraph_t body, cudaGraphConditionalHandle cond, int max_iter) {
   qsft_plan pl = *plan;
   int first = 0, set = 1, mi = max_iter;
-  void* a1[] = {&pl, &first};
+  void* a0[] = {&pl, &first};
+  void* a1[] = {&pl};
   void* a2[] = {&pl, &cond, &set, &mi};
   struct K {
     void* f;
     unsigned grid, block;
     void** args;
-  } ks[] = {{(void*)detect_kernel<T>, DET_BLOCKS, DEC_THREADS, a1},
+  } ks[] = {{(void*)scan_kernel<T>, SCAN_BLOCKS, SCAN_THREADS, a0},
+            {(void*)decode_kernel<T>, DEC_BLOCKS, DEC_THREADS, a1},
             {(void*)peel_kernel<T>, LIST_BLOCKS, PEEL_THREADS, a2}};
   cudaGraphNode_t prev = nullptr;
   for (const K& k : ks) {
@@ -732,9 +787,10 @@ static int run_graph(const qsft_plan* plan, int max_iter, cudaStream_t st) {
 static int check_plan(const qsft_plan* p) {
   if (!p || p->njobs <= 0 || !p->jobs || !p->bin_prefix || !p->i8 || !p->U || !p->rho || !p->ball_best ||
       !p->uniq || !p->ball_tab || !p->ball_k || !p->ball_sum || !p->ball_cnt ||
-      !p->ctrl || !p->roots || !p->bin_status || !p->bin_stamp || !p->dirty || !p->done_count)
+      !p->ctrl || !p->roots || !p->bin_status || !p->bin_stamp || !p->dirty || !p->cand || !p->done_count)
     return QSFT_ERR_ARG;
   if (p->kstride < 16 || (p->kstride & 15) || p->kstride > 2 * QSFT_MAX_N) return QSFT_ERR_ARG;
+  if (p->stage && (p->stage_rp < 1 || p->stage_rp > DEC_STAGE_RP)) return QSFT_ERR_ARG;
   if (p->max_q > QSFT_MAX_Q || p->max_n > QSFT_MAX_N) return QSFT_ERR_TOO_LARGE;
   if (p->prec != QSFT_F32 && p->prec != QSFT_F64) return QSFT_ERR_ARG;
   if (p->total_bins <= 0) return QSFT_ERR_ARG;

@@ -282,7 +282,8 @@ class Batch:
                  block.nbytes,                                                      # packed index arrays
                  bins * 16, slots * 8, balls * 8, balls * 4,                        # rho, ball table, best, uniq
                  balls * ks, balls * 16, balls * 4,                                 # ball k, sum, count
-                 bins, bins * 4, 2 * bins * 4,                                      # status, stamp, dirty
+                 bins, bins * 4, 2 * bins * 4, bins * 4,                            # status, stamp, dirty, cand
+                 (bins // 8) * self.stage_rp() * es,                                # staged candidate columns
                  balls * ks, balls * 16, balls * 4, (2 + 2 * J + cs * J) * 8, 8]    # outputs, metadata, done
         if self.prec == QSFT_F32:
             p = QsftPlan()
@@ -290,6 +291,10 @@ class Batch:
             if self.lib.qsft_gemm_layout(self.jobs_host, J, ctypes.byref(p), index) == 0:
                 sizes.append(max(int(p.gm_ws_bytes), 256))
         return int(sum((s + 511) // 512 * 512 for s in sizes))
+
+    def stage_rp(self):
+        """Column length of the peeling's staging buffer: the longest R*P, at most 64."""
+        return max(1, min(max(s[4] * s[5] for s in self.shapes), 64))
 
     def device_bytes(self):
         """Bytes of this batch's device tensors (what ``planned_bytes`` predicts)."""
@@ -371,6 +376,12 @@ class Batch:
         p.ball_sum, p.ball_cnt, p.ctrl = ptr(self.ball_sum), ptr(self.ball_cnt), ptr(self.ctrl)
         p.bin_status, p.bin_stamp = ptr(self.bin_status), ptr(self.bin_stamp)
         p.dirty = ptr(self.dirty)
+        self.cand = z(self.total_bins, torch.int32)
+        p.cand = ptr(self.cand)
+        # copies of the candidates' columns (1/8 of the bins, R*P <= 64 only)
+        p.stage_rp = self.stage_rp()
+        self.stage = torch.empty(max((self.total_bins // 8) * p.stage_rp, 1), dtype=self.cdt, device=dev)
+        p.stage = ptr(self.stage)
         self.done_count = z(2, torch.int32)
         p.done_count = ptr(self.done_count)
         p.tc_prefix, p.total_tc_work = ptr(self.tc_prefix), self.tc_prefix_host[-1]
