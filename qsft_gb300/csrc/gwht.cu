@@ -400,6 +400,157 @@ static int launch_row(c2<T>* data, const int64_t* row_off, int64_t nrows, int b,
   return QSFT_OK;
 }
 
+// ---------------------------------------------------------------- row-cluster path
+// q in {2, 4}, rows of B = RC_SL * CS values (CS = 2, 4 or 8): a thread-block
+// cluster of CS CTAs per row, CTA r holding the slice [r*RC_SL, (r+1)*RC_SL)
+// in shared memory (RC_SL/16 threads, 16 values each).  Three passes over the
+// slice's 12 low bits (the first reads global memory, coalesced: lanes on
+// consecutive values; the tile is padded by one value per 16 as in the row
+// kernel), then one pass over the top log2(CS) bits across the cluster: each
+// thread takes its CTA's share of the slice offsets, reads the CS values of an
+// offset from the CS slices (distributed shared memory), transforms them, and
+// stores them -- scaled and with the row's device noise -- straight to global
+// memory.  Entries o + RC_SL*k and o + RC_SL*(k + CS/2) are e and e + B/2, so a
+// thread draws one noise pair for both, the same values as the row kernel and
+// the separate noise pass.  A CTA needs a quarter of the row kernel's shared
+// memory, so several rows are in flight on an SM: one row's loads overlap
+// another's butterflies.
+constexpr int RC_SL = 4096;
+constexpr int RC_THREADS = RC_SL / 16;
+
+template <typename T, int Q, int CS>
+__global__ void __launch_bounds__(RC_THREADS, sizeof(T) == 4 ? 4 : 2) gwht_rowc_kernel(c2<T>* __restrict__ data,
+                                                               const int64_t* __restrict__ row_off,
+                                                               const qsft_job* __restrict__ jobs,
+                                                               const int32_t* __restrict__ row_meta) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  extern __shared__ __align__(16) unsigned char smem[];
+  c2<T>* tile = reinterpret_cast<c2<T>*>(smem);
+  const int rank = (int)cluster.block_rank();
+  const int64_t row = blockIdx.x / CS;
+  c2<T>* __restrict__ x = data + __ldg(row_off + row);
+  const c2<T>* __restrict__ xs = x + (int64_t)rank * RC_SL;
+  const int t = threadIdx.x;
+  constexpr int B = RC_SL * CS;
+  const RowNoise nz = [&] {
+    RowNoise r = {make_uint2(0, 0), 0, 0.0};
+    if (jobs) {
+      const qsft_job* jb = jobs + __ldg(row_meta + 2 * row);
+      r.key = noise_key(jb->noise_seed);
+      r.row = __ldg(row_meta + 2 * row + 1);
+      r.nu = jb->noise_nu;
+    }
+    return r;
+  }();
+  c2<T> v[16];
+  // bits [8, 12): e = t + 256 m, from global memory
+#pragma unroll
+  for (int m = 0; m < 16; ++m) v[m] = xs[t + 256 * m];
+  groups_dft<c2<T>, Q, 16>(v);
+#pragma unroll
+  for (int m = 0; m < 16; ++m) tile[pad16(t + 256 * m)] = v[m];
+  __syncthreads();
+  // bits [4, 8): e = (t % 16) + 256 (t / 16) + 16 m
+  {
+    const int base = (t & 15) + ((t >> 4) << 8);
+#pragma unroll
+    for (int m = 0; m < 16; ++m) v[m] = tile[pad16(base + 16 * m)];
+    groups_dft<c2<T>, Q, 16>(v);
+#pragma unroll
+    for (int m = 0; m < 16; ++m) tile[pad16(base + 16 * m)] = v[m];
+  }
+  __syncthreads();
+  // bits [0, 4): e = 16 t + m
+#pragma unroll
+  for (int m = 0; m < 16; ++m) v[m] = tile[pad16(16 * t + m)];
+  groups_dft<c2<T>, Q, 16>(v);
+#pragma unroll
+  for (int m = 0; m < 16; ++m) tile[pad16(16 * t + m)] = v[m];
+  cluster.sync();  // every slice transformed along its low bits
+  // the top log2(CS) bits across the cluster; this CTA's offsets [rank*OPC, (rank+1)*OPC)
+  constexpr int OPC = RC_SL / CS;
+  const c2<T>* part[CS];
+#pragma unroll
+  for (int k = 0; k < CS; ++k) part[k] = cluster.map_shared_rank(tile, k);
+  const T scale = (T)1 / (T)B;
+  const T tnu = (T)nz.nu;
+#pragma unroll 1
+  for (int o = rank * OPC + t; o < (rank + 1) * OPC; o += RC_THREADS) {
+    c2<T> w[CS];
+#pragma unroll
+    for (int k = 0; k < CS; ++k) w[k] = part[k][pad16(o)];
+    if constexpr (CS == Q) {
+      dft_small<c2<T>, Q>(w, nullptr);
+    } else {  // q = 2: the 2-point DFT along each of the log2(CS) binary digits
+#pragma unroll
+      for (int st = CS / 2; st >= 1; st /= 2)
+#pragma unroll
+        for (int k = 0; k < CS; ++k)
+          if (!(k & st)) {
+            const c2<T> a = w[k], c = w[k + st];
+            w[k] = cadd(a, c);
+            w[k + st] = csub(a, c);
+          }
+    }
+#pragma unroll
+    for (int k = 0; k < CS / 2; ++k) {
+      const int64_t e0 = o + (int64_t)RC_SL * k, e1 = e0 + B / 2;
+      c2<T> a = w[k], c = w[k + CS / 2];
+      a.x *= scale;
+      a.y *= scale;
+      c.x *= scale;
+      c.y *= scale;
+      if (nz.nu > 0.0) {
+        c2<T> g0, g1;
+        noise_pair<T>(nz.key, nz.row, B / 2, e0, g0, g1);
+        a.x += tnu * g0.x;
+        a.y += tnu * g0.y;
+        c.x += tnu * g1.x;
+        c.y += tnu * g1.y;
+      }
+      x[e0] = a;
+      x[e1] = c;
+    }
+  }
+  cluster.sync();  // the other CTAs have read this CTA's slice
+}
+
+template <typename T, int Q, int CS>
+static int launch_rowc(c2<T>* data, const int64_t* row_off, int64_t nrows, cudaStream_t st, const qsft_job* jobs,
+                       const int32_t* row_meta) {
+  const size_t sm = (size_t)(RC_SL + RC_SL / 16) * sizeof(c2<T>);
+  auto kern = gwht_rowc_kernel<T, Q, CS>;
+  if (!ensure_smem((const void*)kern, (int)sm)) return QSFT_ERR_CUDA;
+  if (nrows * CS > 0x7fffffffLL) return QSFT_ERR_TOO_LARGE;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(nrows * CS));
+  cfg.blockDim = dim3(RC_THREADS);
+  cfg.dynamicSmemBytes = sm;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CS;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, kern, data, row_off, jobs, row_meta) != cudaSuccess) return QSFT_ERR_CUDA;
+  QSFT_CUDA_CHECK_LAUNCH();
+  return QSFT_OK;
+}
+
+// the row-cluster kernel for B = 2^bits values, q in {2, 4}: bits 13..15 (CS = 2, 4, 8)
+template <typename T>
+static int launch_rowc_bits(int q, int bits, c2<T>* d, const int64_t* row_off, int64_t nrows, cudaStream_t st,
+                            const qsft_job* jobs, const int32_t* row_meta) {
+  if (q == 4 && bits == 14) return launch_rowc<T, 4, 4>(d, row_off, nrows, st, jobs, row_meta);
+  if (q == 2 && bits == 13) return launch_rowc<T, 2, 2>(d, row_off, nrows, st, jobs, row_meta);
+  if (q == 2 && bits == 14) return launch_rowc<T, 2, 4>(d, row_off, nrows, st, jobs, row_meta);
+  if (q == 2 && bits == 15) return launch_rowc<T, 2, 8>(d, row_off, nrows, st, jobs, row_meta);
+  return QSFT_ERR_ARG;
+}
+
 // ---------------------------------------------------------------- cluster path
 // A row of B = q^b values is split over a cluster of CS = q^k CTAs (CTA j holds
 // elements [j*Bp, (j+1)*Bp), Bp = B/CS).  Axes 0..k-1 span the CTAs: their
@@ -680,6 +831,7 @@ static int run_gwht(int q, int b, void* data, const int64_t* row_off, int64_t nr
   if ((q == 2 || q == 4)) {
     const int bits = (q == 4 ? 2 : 1) * b;
     const int maxbits = sizeof(T) == 4 ? 14 : 13;  // whole row in shared memory
+    if (bits >= 13 && bits <= 15) return launch_rowc_bits<T>(q, bits, d, row_off, nrows, st, jobs, row_meta);
     if (bits >= 8 && bits <= maxbits)
       return q == 4 ? launch_row<T, 4>(d, row_off, nrows, b, st, jobs, row_meta)
                     : launch_row<T, 2>(d, row_off, nrows, b, st, jobs, row_meta);
