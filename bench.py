@@ -286,6 +286,13 @@ def run_serving(args, dev):
     reqs = [random_mix_request() for _ in range(N)]
     t_gen = time.perf_counter() - t
     budget = int(args.serve_budget_gb * (1 << 30))
+    # every shape's GWHT schedule tuned before the clock starts (first use would
+    # otherwise time the candidates inside the serving loop)
+    from qsft_gb300 import autotune
+    t = time.perf_counter()
+    for q, b in sorted({(r.q, r.b) for r in reqs}):
+        autotune.ensure(q, b, "fp32", dev)
+    t_tune = time.perf_counter() - t
     ex = GpuExecutor(max_inflight=4, device=dev)
     srv = Server(ex, budget_bytes=budget, max_jobs=32, max_inflight=4)
     srv.run(reqs[:128], np.zeros(128))                  # warm-up: allocator pool, kernel attributes
@@ -352,7 +359,7 @@ def run_serving(args, dev):
             "fp64_plain": {"value": fp64_tps, "unit": UNIT, "sample": n64,
                            "same_support_as_fp32_mix": f"{agree}/{n64}"},
             "batched_fp32_over_fp64_plain": tps / fp64_tps,
-            "nmse_vs_truth": acc, "oracle_pin": pin, "request_generation_s": t_gen,
+            "nmse_vs_truth": acc, "oracle_pin": pin, "request_generation_s": t_gen, "gwht_tuning_s": t_tune,
             "mix": "q{2,3,4,5,20} n[8,60] b[3,8] 40<=q^b<=2^20 S[10,min(2000,q^b/4)] SNR{10,20,inf}dB; "
                    "noisy: NSO R=2, noiseless: identity R=1; C=3"}
 
@@ -593,6 +600,7 @@ def run_ours(args):
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(launches),
         "roofline": roofline, "roofline_gwht": roof_gwht, "clocks": clocks,
+        "gwht_schedules": __import__("qsft_gb300.autotune", fromlist=["table"]).table(),
     }
     if serving is not None:
         line["serving_mix"] = serving

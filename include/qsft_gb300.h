@@ -279,6 +279,40 @@ int qsft_gwht(int prec, int q, int b, void* data, const int64_t* row_off, int64_
 int qsft_gwht_noise(const qsft_plan* plan, int q, int b, const int64_t* row_off, const int32_t* row_meta,
                     int64_t nrows, qsft_stream_t stream);
 
+/*
+ * GWHT schedules: the kernels that can transform rows of one (q, b) shape.
+ *   QSFT_GWHT_ROW           q in {2, 4}, q^b = 2^8..2^14 (FP64 2^13): a CTA per
+ *                           row, whole row in shared memory
+ *   QSFT_GWHT_ROWC          q in {2, 4}, q^b = 2^13..2^15: a thread-block
+ *                           cluster of 4096-value slices per row, the top bits
+ *                           across the cluster through distributed shared memory
+ *   QSFT_GWHT_CLUSTER       rows above 48 KB whose q^k-way split fits 64 KB per
+ *                           CTA (q^k <= 8): any q, radix-q passes per slice
+ *   QSFT_GWHT_PASSES        tile passes through global memory, tiles up to 200 KB
+ *   QSFT_GWHT_PASSES_SMALL  the same with tiles up to 48 KB (more CTAs per SM),
+ *                           for rows above 48 KB
+ * Every schedule gives the same transform (and the same fused noise values).
+ * qsft_gwht and qsft_gwht_noise use the schedule selected for the shape and
+ * precision (process-wide, all devices), else the built-in rule (the first
+ * valid of ROWC, ROW, CLUSTER, PASSES).  No counterpart in the reference,
+ * whose gwht is scipy's fftn: this is the GWHT schedule choice the batched
+ * path makes, normally from a timing of every valid schedule on the device
+ * (qsft_gb300/autotune.py).
+ */
+#define QSFT_GWHT_AUTO 0
+#define QSFT_GWHT_ROW 1
+#define QSFT_GWHT_ROWC 2
+#define QSFT_GWHT_CLUSTER 3
+#define QSFT_GWHT_PASSES 4
+#define QSFT_GWHT_PASSES_SMALL 5
+/* the valid schedules of a shape: their count, the first max_ids written to ids */
+int qsft_gwht_schedules(int prec, int q, int b, int32_t* ids, int max_ids);
+/* select `schedule` (or QSFT_GWHT_AUTO: the built-in rule) for a shape;
+ * QSFT_ERR_ARG when it is not valid for the shape */
+int qsft_gwht_select(int prec, int q, int b, int schedule);
+/* the schedule qsft_gwht and qsft_gwht_noise use for a shape now */
+int qsft_gwht_selected(int prec, int q, int b);
+
 /* ---- bin noise ---------------------------------------------------------- */
 /*
  * Replaces the bin-domain AWGN of SyntheticSubsampledSignal.get_MDU

@@ -24,12 +24,14 @@ NOALLOC_MAX_BINS = 16384   # QSFT_NOALLOC_MAX_BINS
 NOALLOC_KSTRIDE = 32       # QSFT_NOALLOC_KSTRIDE
 TC_SUB_N = 128
 PEEL_LAUNCHES_PER_ITER = 3   # QSFT_PEEL_LAUNCHES_PER_ITER
+GWHT_SCHEDULES = {1: "row", 2: "rowc", 3: "cluster", 4: "passes", 5: "passes_small"}   # QSFT_GWHT_*
 
 # exported symbols, in header order
 SYMBOLS = [
     "qsft_abi_version", "qsft_status_string", "qsft_built_arch", "qsft_launch_count", "qsft_eval_cosets",
     "qsft_eval_cosets_tc", "qsft_eval_cosets_gemm", "qsft_gemm_layout", "qsft_eval_points",
-    "qsft_gwht_noise", "qsft_gwht", "qsft_add_noise_philox", "qsft_add_bins", "qsft_peel_init", "qsft_peel_iteration",
+    "qsft_gwht_noise", "qsft_gwht", "qsft_gwht_schedules", "qsft_gwht_select", "qsft_gwht_selected",
+    "qsft_add_noise_philox", "qsft_add_bins", "qsft_peel_init", "qsft_peel_iteration",
     "qsft_peel_run", "qsft_collect", "qsft_rs_decode", "qsft_peel_noalloc", "qsft_workspace_layout",
 ]
 
@@ -116,6 +118,9 @@ def load():
         "qsft_eval_points": ([i32, i32, i32, i32, vp, i64, vp, vp, vp, vp], i32),
         "qsft_gwht": ([i32, i32, i32, vp, vp, i64, vp], i32),
         "qsft_gwht_noise": ([plan_p, i32, i32, vp, vp, i64, vp], i32),
+        "qsft_gwht_schedules": ([i32, i32, i32, ctypes.POINTER(ctypes.c_int32), i32], i32),
+        "qsft_gwht_select": ([i32, i32, i32, i32], i32),
+        "qsft_gwht_selected": ([i32, i32, i32], i32),
         "qsft_add_noise_philox": ([plan_p, vp], i32),
         "qsft_add_bins": ([i32, vp, vp, i64, vp], i32),
         "qsft_peel_init": ([plan_p, vp], i32),

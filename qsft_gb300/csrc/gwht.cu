@@ -13,6 +13,8 @@
 // exchanged through distributed shared memory).
 #include <cooperative_groups.h>
 
+#include <atomic>
+
 #include "common.cuh"
 #include "noise.cuh"
 
@@ -818,28 +820,65 @@ static int launch_pass(c2<T>* data, const int64_t* row_off, int64_t nrows, int q
   return QSFT_OK;
 }
 
+// ---------------------------------------------------------------- schedules
+// The kernels that can transform rows of a (q, b) shape, chosen per shape:
+// the built-in rule (QSFT_GWHT_AUTO), or the schedule the caller selected
+// with qsft_gwht_select -- normally the winner of a timing of every valid
+// schedule on the device (the autotuner of qsft_gb300/autotune.py).
+static std::atomic<int> g_sched[2][QSFT_MAX_Q + 1][23];  // [FP32, FP64][q][b]
+
+static int rowc_ok(int q, int b) {
+  const int bits = (q == 4 ? 2 : 1) * b;
+  return (q == 4 && bits == 14) || (q == 2 && bits >= 13 && bits <= 15);
+}
+static int row_ok(int q, int b, size_t es) {
+  if (q != 2 && q != 4) return 0;
+  const int bits = (q == 4 ? 2 : 1) * b;
+  return bits >= 8 && bits <= (es == 8 ? 14 : 13);
+}
+static int passes_ok(int q, int b, size_t es, size_t budget) {
+  Pass passes[24];
+  return plan_passes(q, b, es, budget - QSFT_MAX_Q * es, passes, 24) > 0;
+}
+static int sched_valid(int sched, int q, int b, size_t es) {
+  int k = 0;
+  switch (sched) {
+    case QSFT_GWHT_ROW: return row_ok(q, b, es);
+    case QSFT_GWHT_ROWC: return rowc_ok(q, b);
+    case QSFT_GWHT_CLUSTER: return cluster_split(q, b, es, &k) > 0;
+    case QSFT_GWHT_PASSES: return passes_ok(q, b, es, 200 * 1024);
+    case QSFT_GWHT_PASSES_SMALL:  // a plan of its own only for rows above 48 KB
+      return (size_t)ipow(q, b) * es > 48 * 1024 && passes_ok(q, b, es, 48 * 1024);
+    default: return 0;
+  }
+}
+// the built-in rule: the row-cluster kernel, else the row kernel, else a
+// cluster per row, else tile passes through global memory
+static int sched_default(int q, int b, size_t es) {
+  const int order[] = {QSFT_GWHT_ROWC, QSFT_GWHT_ROW, QSFT_GWHT_CLUSTER, QSFT_GWHT_PASSES};
+  for (int s : order)
+    if (sched_valid(s, q, b, es)) return s;
+  return 0;
+}
+
 template <typename T>
 static int run_gwht(int q, int b, void* data, const int64_t* row_off, int64_t nrows, cudaStream_t st,
                     const qsft_job* jobs = nullptr, const int32_t* row_meta = nullptr, int* status_word = nullptr) {
   const size_t es = sizeof(c2<T>);
-  const size_t budget = 200 * 1024 - QSFT_MAX_Q * es;
-  Pass passes[24];
-  const int np = plan_passes(q, b, es, budget, passes, 24);
-  if (np <= 0) return QSFT_ERR_TOO_LARGE;
+  int sched = g_sched[es == 8 ? 0 : 1][q][b].load(std::memory_order_relaxed);
+  if (sched == QSFT_GWHT_AUTO || !sched_valid(sched, q, b, es)) sched = sched_default(q, b, es);
+  if (!sched) return QSFT_ERR_TOO_LARGE;
   c2<T>* d = reinterpret_cast<c2<T>*>(data);
   const T div = (T)ipow(q, b);
-  if ((q == 2 || q == 4)) {
-    const int bits = (q == 4 ? 2 : 1) * b;
-    const int maxbits = sizeof(T) == 4 ? 14 : 13;  // whole row in shared memory
-    if (bits >= 13 && bits <= 15) return launch_rowc_bits<T>(q, bits, d, row_off, nrows, st, jobs, row_meta);
-    if (bits >= 8 && bits <= maxbits)
-      return q == 4 ? launch_row<T, 4>(d, row_off, nrows, b, st, jobs, row_meta)
-                    : launch_row<T, 2>(d, row_off, nrows, b, st, jobs, row_meta);
-  }
-  // other shapes: the noise (jobs non-null) goes into the last pass, one draw per entry
-  int k = 0;
-  const int CS = cluster_split(q, b, es, &k);
-  if (CS > 0) {
+  const int bits = (q == 4 ? 2 : 1) * b;
+  if (sched == QSFT_GWHT_ROWC) return launch_rowc_bits<T>(q, bits, d, row_off, nrows, st, jobs, row_meta);
+  if (sched == QSFT_GWHT_ROW)
+    return q == 4 ? launch_row<T, 4>(d, row_off, nrows, b, st, jobs, row_meta)
+                  : launch_row<T, 2>(d, row_off, nrows, b, st, jobs, row_meta);
+  // other schedules: the noise (jobs non-null) goes into the last pass, one draw per entry
+  if (sched == QSFT_GWHT_CLUSTER) {
+    int k = 0;
+    const int CS = cluster_split(q, b, es, &k);
     switch (q) {
       case 2: return launch_cluster<T, 2>(d, row_off, nrows, q, b, k, CS, div, st, jobs, row_meta, status_word);
       case 3: return launch_cluster<T, 3>(d, row_off, nrows, q, b, k, CS, div, st, jobs, row_meta, status_word);
@@ -848,6 +887,10 @@ static int run_gwht(int q, int b, void* data, const int64_t* row_off, int64_t nr
       default: return launch_cluster<T, 0>(d, row_off, nrows, q, b, k, CS, div, st, jobs, row_meta, status_word);
     }
   }
+  const size_t budget = (sched == QSFT_GWHT_PASSES_SMALL ? 48 : 200) * 1024 - QSFT_MAX_Q * es;
+  Pass passes[24];
+  const int np = plan_passes(q, b, es, budget, passes, 24);
+  if (np <= 0) return QSFT_ERR_TOO_LARGE;
   for (int i = 0; i < np; ++i) {
     const bool last = i == np - 1;
     const T dv = last ? div : (T)1;
@@ -898,4 +941,34 @@ extern "C" int qsft_gwht(int prec, int q, int b, void* data, const int64_t* row_
   if (prec == QSFT_F32) return run_gwht<float>(q, b, data, row_off, nrows, st);
   if (prec == QSFT_F64) return run_gwht<double>(q, b, data, row_off, nrows, st);
   return QSFT_ERR_ARG;
+}
+
+static int prec_es(int prec) { return prec == QSFT_F32 ? 8 : (prec == QSFT_F64 ? 16 : 0); }
+
+extern "C" int qsft_gwht_schedules(int prec, int q, int b, int32_t* ids, int max_ids) {
+  const int es = prec_es(prec);
+  if (!es || q < 2 || q > QSFT_MAX_Q || b < 1 || b > 22 || ipow(q, b) > (1LL << 22) || max_ids < 0) return QSFT_ERR_ARG;
+  int n = 0;
+  for (int s = QSFT_GWHT_ROW; s <= QSFT_GWHT_PASSES_SMALL; ++s)
+    if (sched_valid(s, q, b, (size_t)es)) {
+      if (ids && n < max_ids) ids[n] = s;
+      ++n;
+    }
+  return n;
+}
+
+extern "C" int qsft_gwht_select(int prec, int q, int b, int schedule) {
+  const int es = prec_es(prec);
+  if (!es || q < 2 || q > QSFT_MAX_Q || b < 1 || b > 22 || ipow(q, b) > (1LL << 22)) return QSFT_ERR_ARG;
+  if (schedule != QSFT_GWHT_AUTO && !sched_valid(schedule, q, b, (size_t)es)) return QSFT_ERR_ARG;
+  g_sched[es == 8 ? 0 : 1][q][b].store(schedule, std::memory_order_relaxed);
+  return QSFT_OK;
+}
+
+extern "C" int qsft_gwht_selected(int prec, int q, int b) {
+  const int es = prec_es(prec);
+  if (!es || q < 2 || q > QSFT_MAX_Q || b < 1 || b > 22 || ipow(q, b) > (1LL << 22)) return QSFT_ERR_ARG;
+  int s = g_sched[es == 8 ? 0 : 1][q][b].load(std::memory_order_relaxed);
+  if (s == QSFT_GWHT_AUTO || !sched_valid(s, q, b, (size_t)es)) s = sched_default(q, b, (size_t)es);
+  return s;
 }

@@ -14,7 +14,7 @@ import ctypes
 import numpy as np
 import torch
 
-from . import _lib
+from . import _lib, autotune
 from ._lib import QSFT_F32, QSFT_F64, QsftJob, QsftPlan, QsftCtrl, check, load, stream_handle
 
 EVAL_TILE = 1024  # QSFT_EVAL_TILE
@@ -464,14 +464,17 @@ class Batch:
             raise ValueError(f"unknown evaluation method {method!r}")
 
     def gwht_noise(self, stream=None):
-        """GWHT of every row, with each job's device bin noise added in the same pass."""
+        """GWHT of every row, with each job's device bin noise added in the same pass
+        (each shape's schedule tuned on its first use, see autotune.ensure)."""
         for (q, b), rows in self.gwht_groups.items():
+            autotune.ensure(q, b, self.prec, self.device)
             check(self.lib.qsft_gwht_noise(ctypes.byref(self.plan), q, b, ctypes.c_void_p(rows.data_ptr()),
                                            ctypes.c_void_p(self.gwht_meta[(q, b)].data_ptr()), rows.numel(),
                                            stream_handle(stream)), "qsft_gwht_noise")
 
     def gwht(self, stream=None):
         for (q, b), rows in self.gwht_groups.items():
+            autotune.ensure(q, b, self.prec, self.device)
             check(self.lib.qsft_gwht(self.prec, q, b, ctypes.c_void_p(self.U.data_ptr()),
                                      ctypes.c_void_p(rows.data_ptr()), rows.numel(), stream_handle(stream)),
                   "qsft_gwht")
@@ -642,6 +645,7 @@ def gwht_device(x, q, b, precision=None):
     if not x.is_cuda or not x.is_contiguous() or x.shape[-1] != q ** b:
         raise ValueError("expected a contiguous CUDA tensor whose last dim is q^b")
     nrows = x.numel() // (q ** b)
+    autotune.ensure(q, b, prec, x.device)
     rows = torch.arange(nrows, dtype=torch.int64, device=x.device) * (q ** b)
     check(lib.qsft_gwht(prec, q, b, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(rows.data_ptr()), nrows,
                         stream_handle()), "qsft_gwht")

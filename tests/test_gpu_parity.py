@@ -341,6 +341,62 @@ def test_fused_gwht_noise_equals_separate_passes(cuda, prec):
         assert np.allclose(x, y, rtol=0, atol=1e-6 if prec == "fp32" else 1e-13), j
 
 
+@pytest.mark.parametrize("prec", PRECS)
+@pytest.mark.parametrize("q,b", [(4, 7), (2, 13), (2, 14), (2, 15), (4, 6), (2, 10), (3, 9), (5, 6), (5, 7), (20, 3),
+                                 (20, 4), (4, 8), (16, 4)])
+def test_every_gwht_schedule_vs_oracle(cuda, prec, q, b, monkeypatch):
+    """Each GWHT schedule the library offers for the shape (the autotuner's
+    candidates) gives the reference's gwht, and its fused device noise equals
+    the transform followed by the separate noise pass."""
+    import torch
+    from qsft_gb300 import autotune
+    from qsft_gb300.engine import Batch, JobSpec, gwht_device
+    monkeypatch.setenv("QSFT_GWHT_AUTOTUNE", "0")      # the explicit selections below stand
+    rs = np.random.RandomState(q * 31 + b)
+    x = rs.randn(2, q ** b) + 1j * rs.randn(2, q ** b)
+    want = np.stack([O.gwht(r, q, b) for r in x])
+    P, R, C = 3, 1, 2
+    U = torch.from_numpy(rs.randn(C, R * P, q ** b) + 1j * rs.randn(C, R * P, q ** b))
+    spec = JobSpec(q, P - 1, b, np.zeros((C, P - 1, b)), np.zeros((C, R * P, P - 1)), R, P, U=U, noise_nu=0.3,
+                   noise_seed=5 + q)
+    cands = autotune.schedules(q, b, prec)
+    assert cands
+    fused = []
+    try:
+        for s in cands:
+            autotune.select(q, b, prec, s)
+            t = torch.from_numpy(x).to(cuda).to(torch.complex128 if prec == "fp64" else torch.complex64)
+            got = gwht_device(t, q, b).cpu().numpy()
+            assert rel_err(got, want) < REL[prec] * (3 if q == 20 else 1), s
+            a = Batch([spec], precision=prec)
+            a.gwht(); a.add_noise()
+            b_ = Batch([spec], precision=prec)
+            b_.gwht_noise()
+            assert np.allclose(a.job_U(0).cpu().numpy(), b_.job_U(0).cpu().numpy(), rtol=0,
+                               atol=1e-5 if prec == "fp32" else 1e-13), s
+            fused.append(b_.job_U(0).cpu().numpy())
+    finally:
+        autotune.clear()
+    for f in fused[1:]:                                 # one noise realisation whatever the schedule
+        assert np.allclose(f, fused[0], rtol=0, atol=1e-5 if prec == "fp32" else 1e-12)
+
+
+def test_autotuner_times_every_schedule(cuda):
+    """The tuner times each valid schedule of the shape on the device and
+    selects the fastest."""
+    from qsft_gb300 import autotune
+    try:
+        rec = autotune.tune(4, 7, "fp32")
+        names = [autotune._lib.GWHT_SCHEDULES[s] for s in autotune.schedules(4, 7, "fp32")]
+        assert sorted(rec["times_ms"]) == sorted(names)
+        assert all(0 < v < 100 for v in rec["times_ms"].values())
+        assert rec["times_ms"][rec["name"]] == min(rec["times_ms"].values())
+        assert autotune.selected(4, 7, "fp32") == rec["schedule"]
+        assert rec["rows"] * 4 ** 7 * 8 >= autotune.TUNE_BYTES
+    finally:
+        autotune.clear()
+
+
 def test_batch_of_mixed_shapes_equals_single_runs(cuda):
     """Jobs of different (q, n, b, C, R, P, S) in one packed batch give the
     same results as each alone."""
