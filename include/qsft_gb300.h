@@ -371,6 +371,22 @@ int qsft_peel_run(const qsft_plan* plan, int max_iter, qsft_stream_t stream);
 int qsft_collect(const qsft_plan* plan, uint8_t* out_k, double* out_val, int32_t* out_cnt,
                  int64_t* out_index, int64_t* out_total, qsft_stream_t stream);
 
+/*
+ * Optional FP64 re-projection of every coefficient qsft_collect wrote.  No
+ * counterpart in the reference, whose estimate is the running mean of the
+ * peeling's per-detection projections (qsft/qsft.py:209-217, 247-255): here
+ * every recovered (k, a) is first subtracted from `raw` (a copy of the bins
+ * taken before qsft_peel_init, same layout as plan->U, used as scratch), then
+ * each coefficient becomes the mean over the C groups of
+ * a + <omega^(D_l k), raw_l[:, M_l^T k]> / RP, computed in FP64: the
+ * projection against the raw samples with every other recovered coefficient
+ * removed.  out_k / out_index as qsft_collect wrote them; out_val is
+ * overwritten.  It changes the values the reference returns: the parity path
+ * leaves it off.
+ */
+int qsft_reproject(const qsft_plan* plan, void* raw, const uint8_t* out_k, double* out_val,
+                   const int64_t* out_index, qsft_stream_t stream);
+
 /* ---- Reed-Solomon syndrome decoding ------------------------------------- */
 /*
  * Replaces ReedSolomon.syndrome_decode (qsft/ReedSolomon.py:26-48) for nrows

@@ -20,7 +20,7 @@ __all__ = [
     "random_signal_strength_model", "generate_signal_w", "get_Ms", "get_D", "get_Ms_and_Ds",
     "coset_points", "eval_points", "gwht", "subsample_qsft", "get_MDU_perm", "bin_noise",
     "singleton_detection", "peel", "OracleSignal", "OracleQSFT", "noise_sd_for_snr", "nmse", "closed_form_bins",
-    "test_qary_nmse",
+    "test_qary_nmse", "reproject",
 ]
 
 
@@ -411,3 +411,30 @@ def test_qary_nmse(beta, query_indices, samples, q, n):
     y_hat = np.exp(2j * np.pi * ((X @ keys.T) % q) / q) @ vals
     samples = np.asarray(samples, dtype=np.complex128)
     return float(np.linalg.norm(y_hat - samples) ** 2 / np.linalg.norm(samples) ** 2)
+
+
+def reproject(Us_raw, Ms, Ds, q, gw):
+    """Checker of the optional FP64 re-projection (no counterpart in the
+    reference, which keeps the running mean of qsft/qsft.py:247-255): subtract
+    every (k, a) of `gw` from the raw bins of every group, then re-estimate each
+    a as the mean over the groups of a + <omega^(D_l k), residual column>/len.
+    Us_raw: C arrays (R*P) x B (copied); Ds: C arrays (R*P) x n."""
+    omega = np.exp(2j * np.pi / q)
+    R = [np.array(U, dtype=np.complex128, copy=True) for U in Us_raw]
+    keys = list(gw)
+    K = np.array(keys, dtype=np.int64).reshape(len(keys), -1)
+    a = np.array([gw[k] for k in keys], dtype=np.complex128)
+    bins = []
+    for M, D, U in zip(Ms, Ds, R):
+        b = M.shape[1]
+        j = np.zeros(len(keys), dtype=np.int64)
+        for t in range(b):
+            j = j * q + (K @ M[:, t]) % q
+        sig = omega ** ((np.asarray(D) @ K.T) % q)          # (R*P) x keys
+        np.add.at(U.T, j, -(sig * a).T)
+        bins.append((j, sig))
+    new = np.zeros_like(a)
+    for (j, sig), U in zip(bins, R):
+        new += a + np.sum(np.conjugate(sig) * U[:, j], axis=0) / U.shape[0]
+    new /= len(R)
+    return dict(zip(keys, new))

@@ -32,7 +32,7 @@ SYMBOLS = [
     "qsft_eval_cosets_tc", "qsft_eval_cosets_gemm", "qsft_gemm_layout", "qsft_eval_points",
     "qsft_gwht_noise", "qsft_gwht", "qsft_gwht_schedules", "qsft_gwht_select", "qsft_gwht_selected",
     "qsft_add_noise_philox", "qsft_add_bins", "qsft_peel_init", "qsft_peel_iteration",
-    "qsft_peel_run", "qsft_collect", "qsft_rs_decode", "qsft_peel_noalloc", "qsft_workspace_layout",
+    "qsft_peel_run", "qsft_collect", "qsft_reproject", "qsft_rs_decode", "qsft_peel_noalloc", "qsft_workspace_layout",
 ]
 
 
@@ -127,6 +127,7 @@ def load():
         "qsft_peel_iteration": ([plan_p, i32, vp], i32),
         "qsft_peel_run": ([plan_p, i32, vp], i32),
         "qsft_collect": ([plan_p, vp, vp, vp, vp, vp, vp], i32),
+        "qsft_reproject": ([plan_p, vp, vp, vp, vp, vp], i32),
         "qsft_rs_decode": ([i32, i32, i32, i32, vp, vp, i64, vp, vp], i32),
         "qsft_peel_noalloc": ([i32, ctypes.POINTER(QsftJob), vp, vp, vp, vp, vp, vp, vp, i32, vp, vp], i32),
         "qsft_workspace_layout": ([ctypes.POINTER(QsftJob), i32, ctypes.POINTER(i64), ctypes.POINTER(i64),

@@ -15,7 +15,8 @@ OBJ = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIB = os.path.join(LIBDIR, "libqsft_gb300.so")
 ARCH = "103a"
-SOURCES = ["eval.cu", "eval_tc.cu", "eval_gemm.cu", "gwht.cu", "noise.cu", "peel.cu", "abi.cu", "noalloc.cu"]
+SOURCES = ["eval.cu", "eval_tc.cu", "eval_gemm.cu", "gwht.cu", "noise.cu", "peel.cu", "abi.cu", "noalloc.cu",
+           "reproject.cu"]
 
 
 def nvcc():

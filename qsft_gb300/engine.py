@@ -121,12 +121,13 @@ class JobSpec:
         return sp
 
 
-def workspace_bytes(specs, precision="fp32"):
+def workspace_bytes(specs, precision="fp32", reproject=False):
     """Device bytes a :class:`Batch` of `specs` allocates (its workspace, inputs
     and outputs; not the per-device roots table): the admission footprint of a
     serving loop.  Host-only -- the library's layout functions, no GPU."""
     b = Batch.__new__(Batch)
     b.lib = load()
+    b.reproject = bool(reproject)
     b.prec = precision_code(precision)
     b._build_layout(list(specs))
     return b.planned_bytes()
@@ -145,8 +146,9 @@ class Batch:
     replaces the inputs of a batch with the same layout through pinned host
     staging buffers, so a serving loop re-uses one Batch per layout."""
 
-    def __init__(self, specs, precision="fp32", device=None):
+    def __init__(self, specs, precision="fp32", device=None, reproject=False):
         self.lib = load()
+        self.reproject = bool(reproject)
         specs = list(specs)
         if not specs:
             raise ValueError("empty batch")
@@ -285,6 +287,8 @@ class Batch:
                  bins, bins * 4, 2 * bins * 4, bins * 4,                            # status, stamp, dirty, cand
                  (bins // 8) * self.stage_rp() * es,                                # staged candidate columns
                  balls * ks, balls * 16, balls * 4, (2 + 2 * J + cs * J) * 8, 8]    # outputs, metadata, done
+        if getattr(self, "reproject", False):
+            sizes.append(max(self.n_u, 1) * es)                                      # raw bins copy
         if self.prec == QSFT_F32:
             p = QsftPlan()
             index = (ctypes.c_int64 * (3 * J + 2))()
@@ -391,6 +395,8 @@ class Batch:
         # coset-factored GEMM evaluation (FP32): operand workspace and work index
         # (the layout call fills the plan's gm_* fields; its index is in the block)
         index = (ctypes.c_int64 * (3 * J + 2))()
+        # the bins as they were before the peeling, for the optional re-projection
+        self.U_raw = torch.empty_like(self.U) if getattr(self, "reproject", False) else None
         self.gm_ok = (gm_index is not None and
                       self.lib.qsft_gemm_layout(self.jobs_host, J, ctypes.byref(p), index) == 0)
         if self.gm_ok:
@@ -491,6 +497,10 @@ class Batch:
 
     def peel(self, max_iter=MAX_ITER, stream=None):
         sh = stream_handle(stream)
+        if self.U_raw is not None:
+            st = stream if stream is not None else torch.cuda.current_stream(self.device)
+            with torch.cuda.stream(st):
+                self.U_raw.copy_(self.U)
         check(self.lib.qsft_peel_init(ctypes.byref(self.plan), sh), "qsft_peel_init")
         check(self.lib.qsft_peel_run(ctypes.byref(self.plan), int(max_iter), sh), "qsft_peel_run")
 
@@ -577,6 +587,11 @@ class Batch:
                                     ctypes.c_void_p(self.out_index.data_ptr()),
                                     ctypes.c_void_p(self.out_total.data_ptr()), stream_handle(stream)),
               "qsft_collect")
+        if self.U_raw is not None:   # FP64 re-projection against the raw bins (off on the parity path)
+            check(self.lib.qsft_reproject(ctypes.byref(self.plan), ctypes.c_void_p(self.U_raw.data_ptr()),
+                                          ctypes.c_void_p(self.out_k.data_ptr()), ctypes.c_void_p(self.out_val.data_ptr()),
+                                          ctypes.c_void_p(self.out_index.data_ptr()), stream_handle(stream)),
+                  "qsft_reproject")
 
     def ctrl_host(self, meta=None):
         meta = self._read_meta() if meta is None else meta

@@ -15,7 +15,10 @@ class QSFT:
     reconstruct_method_source ("identity" | "coded"), reconstruct_method_channel
     ("identity" | "nso"), num_subsample, num_repeat, b, source_decoder.
     ``noise_sd`` is accepted and ignored like the reference does.  Extra:
-    ``max_iter`` (default 15, qsft/qsft.py:142)."""
+    ``max_iter`` (default 15, qsft/qsft.py:142); ``reproject`` (default False):
+    re-estimate every recovered coefficient in FP64 against the raw bins with
+    all other recovered coefficients removed (qsft_reproject) instead of the
+    reference's running mean of the peeling's estimates (qsft/qsft.py:247-255)."""
 
     def __init__(self, **kwargs):
         self.reconstruct_method_source = kwargs.get("reconstruct_method_source")
@@ -25,6 +28,7 @@ class QSFT:
         self.b = kwargs.get("b")
         self.source_decoder = kwargs.get("source_decoder", None)
         self.max_iter = kwargs.get("max_iter", MAX_ITER)
+        self.reproject = bool(kwargs.get("reproject", False))
 
     def _rs(self, signal):
         dec = self.source_decoder
@@ -63,7 +67,7 @@ class QSFT:
                        U=U, rs=rs, max_iter=self.max_iter,
                        noise_nu=nz[0] if nz else 0.0, noise_seed=nz[1] if nz else 0)
         peeling_start = time.time()
-        batch = Batch([spec], precision=U.dtype)
+        batch = Batch([spec], precision=U.dtype, reproject=self.reproject)
         if nz:
             batch.add_noise()
         batch.peel(self.max_iter)

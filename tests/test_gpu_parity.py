@@ -397,6 +397,39 @@ def test_autotuner_times_every_schedule(cuda):
         autotune.clear()
 
 
+@pytest.mark.parametrize("prec", PRECS)
+def test_fp64_reprojection_vs_oracle(cuda, prec):
+    """The optional re-projection (qsft_reproject) on a noisy transform equals
+    the oracle's checker applied to the same raw bins and the same peeled
+    estimates; and it does not make the estimates worse against the truth."""
+    import torch
+    from qsft_gb300.engine import Batch
+    from qsft_gb300.serve import random_request
+    np.random.seed(17)
+    req = random_request(4, 14, 5, 120, C=3, R=2, snr_db=10.0)
+    sp = req.spec()
+    sp.noise_nu = 0.0
+    nu = req.noise_sd / np.sqrt(2 * 4 ** 5)
+    noise = np.random.RandomState(3).normal(0, nu, (3, 2 * 15, 4 ** 5, 2)).view(np.complex128)[..., 0]
+    out = []
+    for rp in (False, True):
+        bt = Batch([sp], precision=prec, reproject=rp)
+        bt.eval(); bt.gwht()
+        bt.add_bins(0, torch.from_numpy(noise))
+        raw = bt.job_U(0).cpu().numpy().astype(np.complex128)
+        bt.peel()
+        k, v, _, _ = bt.results()[0]
+        out.append((raw, {tuple(int(x) for x in kk): complex(vv) for kk, vv in zip(k, v)}))
+    (raw, base), (_, got) = out
+    assert set(got) == set(base) and len(base) >= 100
+    Ds = [np.vstack(d) for d in req.Ds]
+    want = O.reproject([raw[c] for c in range(3)], req.Ms, Ds, 4, base)
+    l2 = np.sqrt(sum(abs(got[k] - want[k]) ** 2 for k in want) / sum(abs(x) ** 2 for x in want.values()))
+    assert l2 < (1e-10 if prec == "fp64" else 1e-5), l2
+    truth = {tuple(int(x) for x in kk): complex(a) for kk, a in zip(req.locq.T, req.strengths)}
+    assert O.nmse(truth, got) <= 1.02 * O.nmse(truth, base)
+
+
 def test_batch_of_mixed_shapes_equals_single_runs(cuda):
     """Jobs of different (q, n, b, C, R, P, S) in one packed batch give the
     same results as each alone."""
