@@ -150,10 +150,11 @@ typedef struct qsft_plan {
    * (prec); candidates beyond that share, or jobs with R*P > stage_rp, are read
    * from U.  NULL: no staging.                                                  */
   void* stage;                 /* [(total_bins / 8) * stage_rp] complex             */
-  int32_t* done_count;         /* [2]: [0] jobs whose loop has ended (the peeling
+  int32_t* done_count;         /* [4]: [0] jobs whose loop has ended (the peeling
                                 * kernels exit at once when it reaches njobs);
                                 * [1] blocks of the running peel launch that have
-                                * finished (the last one closes the iteration)     */
+                                * finished (the last one closes the iteration);
+                                * [2], [3] the grid barrier of qsft_peel_persistent */
   /* tensor-core evaluation (FP32 plans): work items are (job, support chunk of
    * tc_smax entries, group of QSFT_TC_TILES tiles of 128 samples)              */
   const int64_t* tc_prefix;    /* [njobs+1] cumulative work items, or NULL          */
@@ -191,6 +192,10 @@ typedef struct qsft_plan {
 #define QSFT_TC_TILES 16
 
 #define QSFT_PLAN_DETERMINISTIC 1  /* reserved */
+/* test only: the grid barriers of qsft_peel_persistent wait for one block more
+ * than the grid has, so that their bounded wait runs out and reports
+ * QSFT_ERR_TIMEOUT in plan->status (the failure path, without a GPU fault) */
+#define QSFT_PLAN_TEST_BARRIER_TIMEOUT 2
 
 /* ---- library ---------------------------------------------------------- */
 int qsft_abi_version(void);                 /* returns 1 */
@@ -354,6 +359,16 @@ int qsft_peel_iteration(const qsft_plan* plan, int first, qsft_stream_t stream);
  * (the condition is set on the device at the end of every iteration).
  */
 int qsft_peel_run(const qsft_plan* plan, int max_iter, qsft_stream_t stream);
+/*
+ * The same loop as one persistent cooperative launch: every block of a grid
+ * the GPU holds at once runs an iteration's scan, decode and peel phases in
+ * turn, with grid-wide barriers between them, and block 0 applies the
+ * stopping rules; the loop ends on the device when every job has left it (or
+ * after max_iter iterations).  No graph node per iteration, no launch between
+ * phases.  Each barrier wait is bounded (2 s): when it runs out the kernel
+ * records QSFT_ERR_TIMEOUT in plan->status (required) and returns.
+ */
+int qsft_peel_persistent(const qsft_plan* plan, int max_iter, qsft_stream_t stream);
 
 /*
  * Gather the result of QSFT.transform for every job: the distinct k recorded

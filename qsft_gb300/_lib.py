@@ -24,6 +24,7 @@ NOALLOC_MAX_BINS = 16384   # QSFT_NOALLOC_MAX_BINS
 NOALLOC_KSTRIDE = 32       # QSFT_NOALLOC_KSTRIDE
 TC_SUB_N = 128
 PEEL_LAUNCHES_PER_ITER = 3   # QSFT_PEEL_LAUNCHES_PER_ITER
+PLAN_TEST_BARRIER_TIMEOUT = 2   # QSFT_PLAN_TEST_BARRIER_TIMEOUT
 GWHT_SCHEDULES = {1: "row", 2: "rowc", 3: "cluster", 4: "passes", 5: "passes_small"}   # QSFT_GWHT_*
 
 # exported symbols, in header order
@@ -32,7 +33,7 @@ SYMBOLS = [
     "qsft_eval_cosets_tc", "qsft_eval_cosets_gemm", "qsft_gemm_layout", "qsft_eval_points",
     "qsft_gwht_noise", "qsft_gwht", "qsft_gwht_schedules", "qsft_gwht_select", "qsft_gwht_selected",
     "qsft_add_noise_philox", "qsft_add_bins", "qsft_peel_init", "qsft_peel_iteration",
-    "qsft_peel_run", "qsft_collect", "qsft_reproject", "qsft_rs_decode", "qsft_peel_noalloc", "qsft_workspace_layout",
+    "qsft_peel_run", "qsft_peel_persistent", "qsft_collect", "qsft_reproject", "qsft_rs_decode", "qsft_peel_noalloc", "qsft_workspace_layout",
 ]
 
 
@@ -126,6 +127,7 @@ def load():
         "qsft_peel_init": ([plan_p, vp], i32),
         "qsft_peel_iteration": ([plan_p, i32, vp], i32),
         "qsft_peel_run": ([plan_p, i32, vp], i32),
+        "qsft_peel_persistent": ([plan_p, i32, vp], i32),
         "qsft_collect": ([plan_p, vp, vp, vp, vp, vp, vp], i32),
         "qsft_reproject": ([plan_p, vp, vp, vp, vp, vp], i32),
         "qsft_rs_decode": ([i32, i32, i32, i32, vp, vp, i64, vp, vp], i32),

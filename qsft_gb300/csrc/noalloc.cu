@@ -38,7 +38,7 @@ constexpr size_t OFF_ROOTS = al(OFF_PREFIX + 2 * sizeof(int64_t));
 constexpr size_t OFF_INDEX = al(OFF_ROOTS + 33 * 32 * 2 * sizeof(double));
 constexpr size_t OFF_CTRL = al(OFF_INDEX + 2 * sizeof(int64_t));
 constexpr size_t OFF_DONE = al(OFF_CTRL + sizeof(qsft_ctrl));
-constexpr size_t OFF_RHO = al(OFF_DONE + 2 * sizeof(int32_t));
+constexpr size_t OFF_RHO = al(OFF_DONE + 4 * sizeof(int32_t));
 constexpr size_t OFF_BALLTAB = al(OFF_RHO + MAX_BINS * 2 * sizeof(double));
 constexpr size_t OFF_BALLBEST = al(OFF_BALLTAB + MAX_SLOTS * sizeof(int64_t));
 constexpr size_t OFF_UNIQ = al(OFF_BALLBEST + MAX_BALLS * sizeof(int64_t));

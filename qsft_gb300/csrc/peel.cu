@@ -257,8 +257,7 @@ constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_BLOCKS = 152 * 8;
 
 template <typename T>
-__global__ void __launch_bounds__(SCAN_THREADS, sizeof(T) == 4 ? 4 : 3) scan_kernel(qsft_plan plan, int first) {
-  if (__ldcg(plan.done_count) >= plan.njobs) return;  // every job has left the loop
+__device__ __forceinline__ void scan_phase(const qsft_plan& plan, int first) {
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
   int64_t chunk0 = 0;  // 32-bin chunks of all jobs are dealt round-robin to the warps
@@ -304,20 +303,26 @@ __global__ void __launch_bounds__(SCAN_THREADS, sizeof(T) == 4 ? 4 : 3) scan_ker
   }
 }
 
+template <typename T>
+__global__ void __launch_bounds__(SCAN_THREADS, sizeof(T) == 4 ? 4 : 3) scan_kernel(qsft_plan plan, int first) {
+  if (__ldcg(plan.done_count) >= plan.njobs) return;  // every job has left the loop
+  scan_phase<T>(plan, first);
+}
+
 // ---------------------------------------------------------------- decode
 // Groups of DEC_G lanes take the candidates of the job's list; each singleton
 // is recorded at once (record_one) and the ball's first detection of the
 // iteration appended to the iteration's list.
 constexpr int DEC_BLOCKS = 152 * 5;   // resident at once (5 blocks of 128 threads per SM)
 
-template <typename T>
-// FP32: 5 blocks per SM (up to 102 registers)
-__global__ void __launch_bounds__(DEC_THREADS, sizeof(T) == 4 ? 5 : 4) decode_kernel(qsft_plan plan) {
-  if (__ldcg(plan.done_count) >= plan.njobs) return;  // every job has left the loop
+// blocks of NT threads (NT / DEC_G bin slots)
+template <typename T, int NT>
+__device__ __forceinline__ void decode_phase(const qsft_plan& plan) {
+  constexpr int NB = NT / DEC_G;
   __shared__ float2 s_w[33 * 32];                            // roots, FP32
-  __shared__ c2<T> s_col[DEC_BINS][DEC_STAGE_RP];
-  __shared__ __align__(16) uint8_t s_k[DEC_BINS][DEC_KB];
-  __shared__ uint8_t s_sym[DEC_BINS][MAX_SYMS];
+  __shared__ c2<T> s_col[NB][DEC_STAGE_RP];
+  __shared__ __align__(16) uint8_t s_k[NB][DEC_KB];
+  __shared__ uint8_t s_sym[NB][MAX_SYMS];
   for (int i = threadIdx.x; i < 33 * 32; i += blockDim.x)
     s_w[i] = make_float2((float)plan.roots[2 * i], (float)plan.roots[2 * i + 1]);
   __syncthreads();
@@ -532,6 +537,13 @@ __global__ void __launch_bounds__(DEC_THREADS, sizeof(T) == 4 ? 5 : 4) decode_ke
   }
 }
 
+template <typename T>
+// FP32: 5 blocks per SM (up to 102 registers)
+__global__ void __launch_bounds__(DEC_THREADS, sizeof(T) == 4 ? 5 : 4) decode_kernel(qsft_plan plan) {
+  if (__ldcg(plan.done_count) >= plan.njobs) return;  // every job has left the loop
+  decode_phase<T, DEC_THREADS>(plan);
+}
+
 // ---------------------------------------------------------------- peel
 // Per job, by one block after every subtraction of the iteration: iteration
 // count, cumulative peel count and the loop's stopping rules (qsft/qsft.py:151,
@@ -575,9 +587,7 @@ __device__ __forceinline__ void sub_entry(double2* p, double dx, double dy) {
 // cut the latency of each item when there are few to overlap.  FP32 plans
 // rotate rho in FP32 (the entries it is subtracted from are FP32).
 template <typename T>
-__global__ void __launch_bounds__(PEEL_THREADS) peel_kernel(qsft_plan plan, cudaGraphConditionalHandle cond,
-                                                           int set_cond, int max_iter) {
-  if (__ldcg(plan.done_count) >= plan.njobs) return;  // every job has left the loop (the same in every block)
+__device__ __forceinline__ void peel_phase(const qsft_plan& plan) {
   __shared__ float2 s_w[33 * 32];                     // FP32 roots, loaded on first use
   bool have_w = false;
   const int lane = threadIdx.x & 31;
@@ -690,6 +700,13 @@ __global__ void __launch_bounds__(PEEL_THREADS) peel_kernel(qsft_plan plan, cuda
       if (fresh) list[pos] = lb;
     }
   }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(PEEL_THREADS) peel_kernel(qsft_plan plan, cudaGraphConditionalHandle cond,
+                                                           int set_cond, int max_iter) {
+  if (__ldcg(plan.done_count) >= plan.njobs) return;  // every job has left the loop (the same in every block)
+  peel_phase<T>(plan);
   // the block that finishes last closes the iteration (every other block's
   // subtractions, list entries and counters are visible to it)
   __shared__ int s_last, s_iter;
@@ -709,6 +726,104 @@ __global__ void __launch_bounds__(PEEL_THREADS) peel_kernel(qsft_plan plan, cuda
     if (set_cond)
       cudaGraphSetConditional(cond, (__ldcg(plan.done_count) < plan.njobs && s_iter < max_iter) ? 1u : 0u);
   }
+}
+
+// ---------------------------------------------------------------- persistent loop
+// The whole loop in one cooperative launch: every block runs the scan, decode
+// and peel phases of an iteration in turn, separated by grid-wide barriers,
+// block 0 closes the iteration between them, and the loop ends when every
+// job has left it (or after max_iter).  The grid is what the GPU holds at once,
+// so every block is resident.  Barrier waits are bounded in time: a wait that
+// runs out records QSFT_ERR_TIMEOUT in plan.status and its block returns (the
+// others then run out at the next barrier); the host reads the status.
+constexpr int LOOP_THREADS = 128;
+constexpr unsigned long long BARRIER_TIMEOUT_NS = 2000000000ull;  // 2 s
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// grid barrier on done_count[2] (arrivals) and done_count[3] (generation)
+__device__ __forceinline__ bool grid_barrier(const qsft_plan& plan, int expected) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile int* gen = plan.done_count + 3;
+    const int g = *gen;
+    __threadfence();
+    s_ok = 1;
+    if (atomicAdd(plan.done_count + 2, 1) == expected - 1) {
+      atomicExch(plan.done_count + 2, 0);
+      __threadfence();
+      atomicAdd(plan.done_count + 3, 1);
+    } else {
+      const unsigned long long t0 = global_ns();
+      while (*gen == g) {
+        if (global_ns() - t0 > BARRIER_TIMEOUT_NS) {
+          s_ok = 0;
+          atomicExch(plan.status, (int)QSFT_ERR_TIMEOUT);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(LOOP_THREADS, 4) peel_loop_kernel(qsft_plan plan, int max_iter) {
+  // test only: a barrier that waits for one block more than the grid has
+  const int expected = (int)gridDim.x + ((plan.flags & QSFT_PLAN_TEST_BARRIER_TIMEOUT) ? 1 : 0);
+  __shared__ int s_iter;
+  for (int it = 0; it < max_iter; ++it) {
+    if (__ldcg(plan.done_count) >= plan.njobs) break;  // the same in every block: read after a barrier
+    scan_phase<T>(plan, it == 0);
+    if (!grid_barrier(plan, expected)) return;
+    decode_phase<T, LOOP_THREADS>(plan);
+    if (!grid_barrier(plan, expected)) return;
+    peel_phase<T>(plan);
+    if (!grid_barrier(plan, expected)) return;
+    if (blockIdx.x == 0) {
+      if (threadIdx.x == 0) s_iter = 0;
+      __syncthreads();
+      end_iteration(plan, &s_iter);
+    }
+    if (!grid_barrier(plan, expected)) return;
+  }
+}
+
+template <typename T>
+static int run_persistent(const qsft_plan* plan, int max_iter, cudaStream_t st) {
+  static int sms[128], per[2][128];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 128) return QSFT_ERR_CUDA;
+  const int pi = sizeof(T) == 4 ? 0 : 1;
+  if (!sms[dev] && cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return QSFT_ERR_CUDA;
+  if (!per[pi][dev] &&
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per[pi][dev], peel_loop_kernel<T>, LOOP_THREADS, 0) != cudaSuccess)
+    return QSFT_ERR_CUDA;
+  if (per[pi][dev] < 1) return QSFT_ERR_TOO_LARGE;
+  qsft_plan pl = *plan;
+  int mi = max_iter;
+  void* args[] = {&pl, &mi};
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(sms[dev] * per[pi][dev]));
+  cfg.blockDim = dim3(LOOP_THREADS);
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelExC(&cfg, (const void*)peel_loop_kernel<T>, args) != cudaSuccess) return QSFT_ERR_CUDA;
+  QSFT_CUDA_CHECK_LAUNCH();
+  return QSFT_OK;
 }
 
 template <typename T>
@@ -811,7 +926,7 @@ extern "C" int qsft_peel_init(const qsft_plan* plan, qsft_stream_t stream) {
       cudaMemsetAsync(plan->ball_sum, 0, sizeof(double) * 2 * plan->total_balls, st) != cudaSuccess ||
       cudaMemsetAsync(plan->ball_cnt, 0, sizeof(int32_t) * plan->total_balls, st) != cudaSuccess ||
       cudaMemsetAsync(plan->bin_stamp, 0, sizeof(int32_t) * plan->total_bins, st) != cudaSuccess ||
-      cudaMemsetAsync(plan->done_count, 0, 2 * sizeof(int32_t), st) != cudaSuccess)
+      cudaMemsetAsync(plan->done_count, 0, 4 * sizeof(int32_t), st) != cudaSuccess)
     return QSFT_ERR_CUDA;
   return QSFT_OK;
 }
@@ -838,4 +953,14 @@ extern "C" int qsft_peel_run(const qsft_plan* plan, int max_iter, qsft_stream_t 
     if (r != QSFT_OK) return r;
   }
   return QSFT_OK;
+}
+
+extern "C" int qsft_peel_persistent(const qsft_plan* plan, int max_iter, qsft_stream_t stream) {
+  if (max_iter < 0) return QSFT_ERR_ARG;
+  if (max_iter == 0) return QSFT_OK;
+  const int rc = check_plan(plan);
+  if (rc != QSFT_OK) return rc;
+  if (!plan->status) return QSFT_ERR_ARG;  // a barrier that runs out reports there
+  cudaStream_t st = (cudaStream_t)stream;
+  return plan->prec == QSFT_F32 ? run_persistent<float>(plan, max_iter, st) : run_persistent<double>(plan, max_iter, st);
 }

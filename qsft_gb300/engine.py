@@ -146,9 +146,12 @@ class Batch:
     replaces the inputs of a batch with the same layout through pinned host
     staging buffers, so a serving loop re-uses one Batch per layout."""
 
-    def __init__(self, specs, precision="fp32", device=None, reproject=False):
+    def __init__(self, specs, precision="fp32", device=None, reproject=False, peel_mode="graph"):
         self.lib = load()
         self.reproject = bool(reproject)
+        if peel_mode not in ("graph", "persistent"):
+            raise ValueError(f"unknown peel_mode {peel_mode!r}")
+        self.peel_mode = peel_mode
         specs = list(specs)
         if not specs:
             raise ValueError("empty batch")
@@ -286,7 +289,7 @@ class Batch:
                  balls * ks, balls * 16, balls * 4,                                 # ball k, sum, count
                  bins, bins * 4, 2 * bins * 4, bins * 4,                            # status, stamp, dirty, cand
                  (bins // 8) * self.stage_rp() * es,                                # staged candidate columns
-                 balls * ks, balls * 16, balls * 4, (2 + 2 * J + cs * J) * 8, 8]    # outputs, metadata, done
+                 balls * ks, balls * 16, balls * 4, (2 + 2 * J + cs * J) * 8, 16]   # outputs, metadata, done
         if getattr(self, "reproject", False):
             sizes.append(max(self.n_u, 1) * es)                                      # raw bins copy
         if self.prec == QSFT_F32:
@@ -386,7 +389,7 @@ class Batch:
         p.stage_rp = self.stage_rp()
         self.stage = torch.empty(max((self.total_bins // 8) * p.stage_rp, 1), dtype=self.cdt, device=dev)
         p.stage = ptr(self.stage)
-        self.done_count = z(2, torch.int32)
+        self.done_count = z(4, torch.int32)
         p.done_count = ptr(self.done_count)
         p.tc_prefix, p.total_tc_work = ptr(self.tc_prefix), self.tc_prefix_host[-1]
         p.tc_smax, p.tc_npad, p.tc_table_bytes = self.tc_smax, self.tc_npad, self.tc_table_bytes
@@ -502,7 +505,10 @@ class Batch:
             with torch.cuda.stream(st):
                 self.U_raw.copy_(self.U)
         check(self.lib.qsft_peel_init(ctypes.byref(self.plan), sh), "qsft_peel_init")
-        check(self.lib.qsft_peel_run(ctypes.byref(self.plan), int(max_iter), sh), "qsft_peel_run")
+        if self.peel_mode == "persistent":   # the loop in one cooperative launch
+            check(self.lib.qsft_peel_persistent(ctypes.byref(self.plan), int(max_iter), sh), "qsft_peel_persistent")
+        else:                                # a launch per phase; a WHILE node when captured
+            check(self.lib.qsft_peel_run(ctypes.byref(self.plan), int(max_iter), sh), "qsft_peel_run")
 
     # ------------------------------------------------------------ whole step
     def step(self, max_iter=None, stream=None):
