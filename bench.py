@@ -50,6 +50,8 @@ def parse():
     p.add_argument("--batch", type=int, default=16)
     p.add_argument("--precision", default="fp32")
     p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--peel-mode", default="graph", choices=["graph", "persistent"],
+                   help="peeling loop: a launch per phase (WHILE node in the captured step) or one persistent launch")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--serve-requests", type=int, default=10000, help="serving-mix requests (0: skip)")
     p.add_argument("--serve-rate", type=float, default=0.0,
@@ -388,7 +390,7 @@ def run_ours(args):
     max_over_ranks = RP.max_over_ranks
 
     # ---- device-resident throughput (value) + per-kernel timing
-    batch = Batch([r.spec() for r in reqs], precision=args.precision, device=dev)
+    batch = Batch([r.spec() for r in reqs], precision=args.precision, device=dev, peel_mode=args.peel_mode)
     stream = torch.cuda.current_stream()
     ev = {k: (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for k in ("eval", "gwht+noise", "peel", "collect")}
@@ -421,7 +423,7 @@ def run_ours(args):
     batch.capture()                         # one CUDA graph per step
     # a second workspace with the same inputs: the timed steps alternate between
     # the two on two streams, two batches in flight as in the end-to-end run
-    batch2 = Batch([r.spec() for r in reqs], precision=args.precision, device=dev)
+    batch2 = Batch([r.spec() for r in reqs], precision=args.precision, device=dev, peel_mode=args.peel_mode)
     batch2.capture()
     streams = (torch.cuda.Stream(dev), torch.cuda.Stream(dev))
     pair = (batch, batch2)
@@ -599,7 +601,7 @@ def run_ours(args):
         "scaling": "weak", "vs_baseline": None, "dtype": "f32" if args.precision == "fp32" else "f64",
         "data": "synthetic (seeded, reference generators)",
         "config": {"workload": "q4_n20_b7_C3_nso_R2_S1000_10dB", **WORKLOAD, "batch": J,
-                   "parallelism": f"replicas x{world}", "l2": "inputs > L2 (bins %.0f MB/step)" %
+                   "parallelism": f"replicas x{world}", "peel_mode": args.peel_mode, "l2": "inputs > L2 (bins %.0f MB/step)" %
                    (samples * 8 * J / 1e6)},
         "value_note": "inputs resident on the device; steps alternate between two captured workspaces on two "
                       "streams (two batches in flight, the overlap e2e also has)",
