@@ -470,42 +470,20 @@ __global__ void __launch_bounds__(RC_THREADS, sizeof(T) == 4 ? 4 : 2) gwht_rowc_
 #pragma unroll
   for (int m = 0; m < 16; ++m) tile[pad16(16 * t + m)] = v[m];
   cluster.sync();  // every slice transformed along its low bits
-  // the top log2(CS) bits across the cluster; this CTA's offsets [rank*OPC, (rank+1)*OPC):
-  // every value the thread needs is read from the CS slices first, then the
-  // cluster barrier is arrived at (relaxed: it only says that this CTA has
-  // finished reading the others' shared memory) and waited for only after the
-  // transforms, the noise and the stores
+  // the top log2(CS) bits across the cluster; this CTA's offsets [rank*OPC, (rank+1)*OPC)
   constexpr int OPC = RC_SL / CS;
-  constexpr int NO = OPC / RC_THREADS;  // offsets per thread; NO * CS == 16
-  static_assert(NO * CS == 16, "16 values per thread");
+  const c2<T>* part[CS];
 #pragma unroll
-  for (int k = 0; k < CS; ++k) {
-    const c2<T>* part = cluster.map_shared_rank(tile, k);
-#pragma unroll
-    for (int i = 0; i < NO; ++i) v[i * CS + k] = part[pad16(rank * OPC + t + RC_THREADS * i)];
-  }
-  // the arrive takes a sum of every loaded value as an input, so it cannot be
-  // issued before all of this thread's reads of the other slices have returned
-  T dep = 0;
-#pragma unroll
-  for (int i = 0; i < 16; ++i) dep += v[i].x;
-  if constexpr (sizeof(T) == 4)
-    asm volatile("barrier.cluster.arrive.relaxed.aligned; // %0" ::"f"(dep) : "memory");
-  else
-    asm volatile("barrier.cluster.arrive.relaxed.aligned; // %0" ::"d"(dep) : "memory");
+  for (int k = 0; k < CS; ++k) part[k] = cluster.map_shared_rank(tile, k);
   const T scale = (T)1 / (T)B;
   const T tnu = (T)nz.nu;
+#pragma unroll 1
+  for (int o = rank * OPC + t; o < (rank + 1) * OPC; o += RC_THREADS) {
+    c2<T> w[CS];
 #pragma unroll
-  for (int i = 0; i < NO; ++i) {
-    const int o = rank * OPC + t + RC_THREADS * i;
-    c2<T>* w = v + i * CS;
+    for (int k = 0; k < CS; ++k) w[k] = part[k][pad16(o)];
     if constexpr (CS == Q) {
-      c2<T> u[CS];
-#pragma unroll
-      for (int k = 0; k < CS; ++k) u[k] = w[k];
-      dft_small<c2<T>, Q>(u, nullptr);
-#pragma unroll
-      for (int k = 0; k < CS; ++k) w[k] = u[k];
+      dft_small<c2<T>, Q>(w, nullptr);
     } else {  // q = 2: the 2-point DFT along each of the log2(CS) binary digits
 #pragma unroll
       for (int st = CS / 2; st >= 1; st /= 2)
@@ -537,7 +515,7 @@ __global__ void __launch_bounds__(RC_THREADS, sizeof(T) == 4 ? 4 : 2) gwht_rowc_
       x[e1] = c;
     }
   }
-  asm volatile("barrier.cluster.wait.aligned;" ::: "memory");  // the others have read this CTA's slice
+  cluster.sync();  // the other CTAs have read this CTA's slice
 }
 
 template <typename T, int Q, int CS>
