@@ -36,7 +36,7 @@ namespace qsft {
 
 constexpr int PEEL_THREADS = 256;
 constexpr int MAX_SYMS = 256;  // channel symbols per bin (P - 1 <= 256)
-constexpr int LIST_BLOCKS = 152 * 8;
+constexpr int LIST_BLOCKS = 152 * 3;   // the peel kernel's grid: resident at once (3 blocks of 256 threads per SM)
 
 // ---------------------------------------------------------------- helpers
 __device__ __forceinline__ uint32_t hash_row(const uint8_t* row, int words) {
@@ -254,7 +254,7 @@ __device__ __forceinline__ c2<T>* stage_col(const qsft_plan& plan, int jid, int 
 // buffer at once -- the values are still in L2 -- so that the decoder reads
 // one contiguous column instead of RP scattered sectors from HBM.
 constexpr int SCAN_THREADS = 256;
-constexpr int SCAN_BLOCKS = 152 * 8;
+constexpr int SCAN_BLOCKS = 152 * 4;   // resident at once (4 blocks of 256 threads per SM)
 
 template <typename T>
 __device__ __forceinline__ void scan_phase(const qsft_plan& plan, int first) {
@@ -277,16 +277,18 @@ __device__ __forceinline__ void scan_phase(const qsft_plan& plan, int first) {
     const c2<T>* U = reinterpret_cast<const c2<T>*>(plan.U) + job->off_U;
     for (int ch = start; ch < nch; ch += nw) {   // uniform over the warp
       const int i = ch * 32 + lane;
-      bool is_cand = false;
+      bool is_cand = false, was_multi = false;
       int local = 0;
       if (i < cnt) {
         local = first ? i : list[i];
         const int64_t gb = job->off_bin + local;
-        if (!first && plan.bin_status[gb] == 1) atomicSub(&ctl->n_multi, 1);
+        was_multi = !first && plan.bin_status[gb] == 1;
         plan.bin_status[gb] = 0;
         const int c = local / B, jb = local - (local / B) * B;
         is_cand = col_energy<T>(U + (int64_t)c * RP * B + jb, RP, B, thr) > thr;
       }
+      const unsigned nm = __ballot_sync(0xffffffffu, was_multi);   // multitons re-classified: one atomic per warp
+      if (lane == 0 && nm) atomicSub(&ctl->n_multi, __popc(nm));
       const int pos = warp_append(is_cand, jid, &ctl->n_cand);
       if (is_cand) plan.cand[job->off_bin + pos] = local;
       for (unsigned m = __ballot_sync(0xffffffffu, is_cand); m; m &= m - 1) {
@@ -528,7 +530,14 @@ __device__ __forceinline__ void decode_phase(const qsft_plan& plan) {
           plan.rho[2 * gb + 1] = rho.y;
           bid = record_one(plan, job, ctl, kl, local, rho, iter, ks, firstb);
         }
-        atomicAdd(single ? &ctl->n_single : &ctl->n_multi, 1);
+      }
+      {  // the class counts, one atomic per warp and counter
+        const unsigned ns = __ballot_sync(0xffffffffu, active && gi == 0 && single);
+        const unsigned nm = __ballot_sync(0xffffffffu, active && gi == 0 && !single);
+        if (lane == 0) {
+          if (ns) atomicAdd(&ctl->n_single, __popc(ns));
+          if (nm) atomicAdd(&ctl->n_multi, __popc(nm));
+        }
       }
       const int pos = warp_append(firstb, jid, &ctl->n_unique);   // the iteration's list of balls
       if (firstb) plan.uniq[job->off_ball + pos] = bid;
@@ -601,7 +610,7 @@ __device__ __forceinline__ void peel_phase(const qsft_plan& plan) {
     const int C = job->C;
     const int cnt = ctl->n_unique * C;
     const int G = cnt >= PEEL_THREAD_MIN ? 1 : DEC_G, cpw = 32 / G, gi = lane % G;
-    if (G > 1 && !have_w) {  // uniform over the block: every thread sees the same counts
+    if (G > 1 && !have_w && cnt > 0) {  // uniform over the block: every thread sees the same counts
       for (int i = threadIdx.x; i < 33 * 32; i += blockDim.x)
         s_w[i] = make_float2((float)plan.roots[2 * i], (float)plan.roots[2 * i + 1]);
       __syncthreads();
