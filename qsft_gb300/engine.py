@@ -105,8 +105,9 @@ class JobSpec:
     @classmethod
     def trusted(cls, q, n, b, M, D, R, P, chan, src, cutoff, K, A, rs, max_iter, noise_nu, noise_seed):
         """A JobSpec from arrays that already passed __init__'s conversions and
-        checks (int64 M (C, n, b), D (C, R*P, n), K (S, n); complex128 A): the
-        per-submit path of a request whose arrays were validated once."""
+        checks (M (C, n, b), D (C, R*P, n), K (S, n) as int64 or int8 digits;
+        complex128 A): the per-submit path of a request whose arrays were
+        validated once."""
         sp = cls.__new__(cls)
         sp.q, sp.n, sp.b, sp.R, sp.P = q, n, b, R, P
         sp.M, sp.D, sp.C = M, D, M.shape[0]
@@ -594,7 +595,12 @@ class Batch:
                                     ctypes.c_void_p(self.out_total.data_ptr()), stream_handle(stream)),
               "qsft_collect")
         if self.U_raw is not None:   # FP64 re-projection against the raw bins (off on the parity path)
-            check(self.lib.qsft_reproject(ctypes.byref(self.plan), ctypes.c_void_p(self.U_raw.data_ptr()),
+            # its scratch is a copy of the raw bins in U (free once the peeling is
+            # collected), so the pristine copy serves every later collection too
+            st = stream if stream is not None else torch.cuda.current_stream(self.device)
+            with torch.cuda.stream(st):
+                self.U.copy_(self.U_raw)
+            check(self.lib.qsft_reproject(ctypes.byref(self.plan), ctypes.c_void_p(self.U.data_ptr()),
                                           ctypes.c_void_p(self.out_k.data_ptr()), ctypes.c_void_p(self.out_val.data_ptr()),
                                           ctypes.c_void_p(self.out_index.data_ptr()), stream_handle(stream)),
                   "qsft_reproject")

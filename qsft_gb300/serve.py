@@ -56,8 +56,10 @@ class TransformRequest:
             sp = JobSpec(self.q, self.n, self.b, np.stack(self.Ms), D, R, P, chan=self.chan, src=self.src,
                          cutoff=self.cutoff, K=self.locq.T, A=self.strengths, rs=rs, max_iter=self.max_iter,
                          noise_nu=nu, noise_seed=self.noise_seed)
-            self._arrays = (sp.M, sp.D, sp.K, sp.A, rs)
-            return sp
+            # int8 digits (checked to lie in 0..127 above): the batch's packing is then a
+            # plain byte copy on every later submit instead of a conversion
+            self._arrays = (np.ascontiguousarray(sp.M, dtype=np.int8), np.ascontiguousarray(sp.D, dtype=np.int8),
+                            np.ascontiguousarray(sp.K, dtype=np.int8), sp.A, rs)
         M, D, K, A, rs = self._arrays
         return JobSpec.trusted(self.q, self.n, self.b, M, D, R, P, self.chan, self.src, self.cutoff, K, A, rs,
                                self.max_iter, nu, self.noise_seed)
