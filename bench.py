@@ -246,8 +246,9 @@ def pin_summary(recs):
 
 
 # DRAM bytes per launch from one ncu capture of this workload (dram__bytes_read.sum +
-# dram__bytes_write.sum; profiles/eval_gemm_q4n20b7_batch16.md, profiles/gwht_row_q4n20b7_batch16.md)
-NCU_TRAFFIC = {"eval": (35.07e6 + 203.33e6) + (12.94e6 + 12.53e6), "gwht": 267.81e6 + 216.15e6, "batch": 16}
+# dram__bytes_write.sum; profiles/eval_gemm_q4n20b7_batch16.md for the GEMM kernel, an
+# earlier capture for its operand kernel, profiles/gwht_rowc_q4n20b7_batch16.md)
+NCU_TRAFFIC = {"eval": (35.07e6 + 202.97e6) + (12.94e6 + 12.53e6), "gwht": 264.32e6 + 203.06e6, "batch": 16}
 
 
 def run_reference(args):
@@ -590,7 +591,10 @@ def run_ours(args):
                 "issued_tflops": None if issued is None else issued / (e_ms / 1e3) / 1e12}
     roofline["frac"] = roofline["achieved"] / roofline["peak"]
     roofline["traffic_unit"] = "bytes per launch (ncu, prep + GEMM kernels)"
-    roof_gwht = {"kernel": "gwht_row (transform + bin noise, one read and one write)", "bound": "hbm", "achieved": gwht_bytes / (g_ms / 1e3) / 1e9, "peak": hbm,
+    from qsft_gb300 import autotune
+    sched = _lib.GWHT_SCHEDULES.get(autotune.selected(w["q"], w["b"], args.precision), "?")
+    roof_gwht = {"kernel": f"gwht, schedule {sched} (transform + bin noise, one read and one write)", "bound": "hbm",
+                 "achieved": gwht_bytes / (g_ms / 1e3) / 1e9, "peak": hbm,
                  "unit": "GB/s", "traffic": NCU_TRAFFIC["gwht"] * J / NCU_TRAFFIC["batch"],
                  "algorithmic_bytes": gwht_bytes,
                  "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
