@@ -184,7 +184,7 @@ typedef struct qsft_plan {
   int32_t gm_nw;               /* 32-bit words of packed b-digit vectors (1, 2, 4)  */
   int32_t gm_npmax;            /* largest N extent: 4 columns per delay row of a
                                 * chunk (<= 56 rows, equal chunks), rounded to 16   */
-  int32_t gm_jt_bytes;         /* shared-memory bytes of the largest j table        */
+  int32_t gm_jt_bytes;         /* shared-memory bytes of the largest group table    */
   int32_t gm_nacc;             /* accumulator buffers in tensor memory (1 or 2)     */
 } qsft_plan;
 

@@ -26,29 +26,36 @@
 //   KPS = 4:                A[l][4s..4s+3] = [Whr, Whi, Wlr, Wli]
 //     B rows repeat the two KPS = 2 rows for the W_lo entries.
 // The epilogue adds the hi and lo columns.  Putting the C halves on N rather
-// than K keeps K at 2 (or 4) entries per support vector, so each MMA reads
-// fewer operand bytes from shared memory per multiply-add: that read rate,
-// not the multiplier array, bounds a single-CTA MMA with N <= 256.  Delay rows
-// go in equal chunks of at most 56 (N <= 224, so two accumulator buffers of a
-// 128-row tile still fit tensor memory).  An operand kernel writes B (and the
-// packed j_s digits) into a workspace in the exact shared-memory image of each
-// 64-entry K chunk (128-byte-swizzled K-major rows), so the GEMM kernel streams
-// it with one bulk copy per chunk.  The GEMM kernel generates A in tensor
-// memory from the row's digits (two dp4a per support vector for b <= 8) and
-// issues tcgen05.mma kind::f16 (M = 128, N, K = 16) into tensor memory.
+// than K keeps K at 2 (or 4) entries per support vector and makes each MMA
+// wide: halves on K (per K step two MMAs of half the N, each reading the same
+// A, into one accumulator) measured 27% slower for the whole evaluation, and
+// accumulating the lo products into the hi accumulator lost FP32 accuracy
+// for q = 20.  Delay rows go in equal chunks of at most 56
+// (N <= 224, so two accumulator buffers of a 128-row tile still fit tensor
+// memory).  An operand kernel writes B (and the group's table) into a
+// workspace in the exact shared-memory image of each 64-entry K chunk
+// (128-byte-swizzled K-major rows), so the GEMM kernel streams it with one
+// bulk copy per chunk.  The GEMM kernel generates A in tensor memory from the
+// row's digits (two dp4a per support vector for b <= 8) and issues
+// tcgen05.mma kind::f16 (M = 128, N, K = 16) into tensor memory.
 //
 // Work unit: MT tiles of 128 rows of one (job, group, chunk of delay rows).
 // The GEMM kernel is persistent (one CTA per SM; units taken from a global
-// counter) with four roles: producer warps (one thread per row) write A chunks
-// into a tensor-memory ring, one warp issues the MMAs, one warp streams the B
-// chunks into a shared-memory ring with bulk copies (and hands out the units),
-// and epilogue warps read the accumulators back (tcgen05.ld) and store U.
-// mbarriers: afull (producers wrote A) / bfull (bulk copy landed), one "chunk
-// consumed" barrier per B slot that frees both rings (one commit per chunk),
-// accf (a unit's MMAs completed) / acce (its accumulators were read), and the
-// unit queue's full / empty.  Every wait is bounded; on a timeout the CTA sets
-// plan.status, drains its copies and MMAs (bounded) and frees its tensor
-// memory.
+// counter) with three roles: two sets of producer warps (one thread per row
+// in each) write the two halves of every A chunk into a tensor-memory ring,
+// the second set also reading each unit's accumulators back (tcgen05.ld) and
+// storing U; one warp issues the MMAs; one warp streams the B chunks into a
+// shared-memory ring with bulk copies (and hands out the units, decoded once
+// into a shared-memory queue, each with its group's table of j_s digits and
+// FP16 roots copied into one of two table buffers).  A chunk takes a producer
+// about as long as its MMAs take the tensor pipe, so one set alone (the
+// epilogue warps idle between drains) left the MMA warp waiting for A.
+// mbarriers: afull (both producer sets wrote an A chunk) / bfull (bulk copy
+// landed), one "chunk consumed" barrier per B slot that frees both rings (one
+// commit per chunk), accf (a unit's MMAs completed) / acce (its accumulators
+// were read), the unit queue's full / empty and the table buffers' full /
+// empty.  Every wait is bounded; on a timeout the CTA sets plan.status, drains
+// its copies and MMAs (bounded) and frees its tensor memory.
 #include "common.cuh"
 #include "tcgen05.cuh"
 
@@ -58,22 +65,26 @@ using namespace qsft::tc;
 
 constexpr int KC = 64;                     // K entries per stage: one 128-byte row (4 MMAs of K = 16)
 constexpr int TM = 128;                    // rows per MMA tile
-constexpr int HDR = 1024;                  // barriers, TMEM slot, flags, root table
+constexpr int HDR = 2048;                  // barriers, TMEM slot, flags, unit queue
+constexpr int UNIT_OFF = 1024;             // unit queue: UQ decoded units of UNIT_BYTES
+constexpr int UNIT_BYTES = 128;
 constexpr int A_COLS = KC / 2;             // TMEM columns of one tile's A chunk (two FP16 per column)
 constexpr int PREP_S = 32;                 // support vectors per operand block
 constexpr int REGION_HDR = 256;            // per-job header (inverse scale; the first also the unit counter)
 constexpr int SCHED_OFF = 8;               // byte offset of the GEMM kernel's work-unit counter in gm_ws
+constexpr int TAB_HDR = 256;               // a group's table: FP16 (hi, lo) roots omega^m, m < 32, then j_s words
 constexpr int MAX_SMEM = 227 * 1024;
 
 constexpr int RPC_MAX = 56;                // delay rows per N chunk (N = 4 columns each, <= 224)
 
 struct Geo {
-  int RPC, nch;      // delay rows per chunk, chunks
-  int NP;            // N extent: 4*RPC rounded up to 16
-  int S_pad, nK;     // support vectors padded to whole stages, K chunks
-  uint32_t CB;       // bytes of one B chunk image (NP x KC FP16)
-  int64_t jt_bytes;  // j table of a group, 256-aligned
-  int64_t region_c;  // bytes per group: j table + nch x nK B chunks
+  int RPC, nch;       // delay rows per chunk, chunks
+  int NP;             // N extent: 4*RPC rounded up to 16
+  int S_pad, nK;      // support vectors padded to whole stages, K chunks
+  uint32_t CB;        // bytes of one B chunk image (NP x KC FP16)
+  uint32_t tab_copy;  // bytes of a group's table the GEMM kernel copies (roots + j words)
+  int64_t tab_bytes;  // the table's bytes in the workspace, 256-aligned
+  int64_t region_c;   // bytes per group: table + nch x nK B chunks
 };
 __host__ __device__ inline Geo geo(int RP, int S, int kps, int nw) {
   Geo g;
@@ -84,10 +95,13 @@ __host__ __device__ inline Geo geo(int RP, int S, int kps, int nw) {
   g.S_pad = (S + spc - 1) / spc * spc;
   g.nK = g.S_pad * kps / KC;
   g.CB = (uint32_t)g.NP * KC * 2;
-  g.jt_bytes = ((int64_t)g.S_pad * nw * 4 + 255) / 256 * 256;
-  g.region_c = g.jt_bytes + (int64_t)g.nch * g.nK * g.CB;
+  g.tab_copy = (uint32_t)(TAB_HDR + g.S_pad * nw * 4);  // S_pad is a multiple of 16: a multiple of 16 bytes
+  g.tab_bytes = ((int64_t)g.tab_copy + 255) / 256 * 256;
+  g.region_c = g.tab_bytes + (int64_t)g.nch * g.nK * g.CB;
   return g;
 }
+// shared-memory bytes of one table buffer for the largest table (keeps the B ring 1024-byte aligned)
+__host__ __device__ inline int tab_smem(const Geo& g) { return (int)((g.tab_copy + 1023) / 1024 * 1024); }
 __host__ __device__ inline int64_t region_bytes(const Geo& g, int C) { return REGION_HDR + (int64_t)C * g.region_c; }
 
 // Operand tiles use the 128-byte-swizzled K-major layout: a row of a tile is
@@ -117,8 +131,9 @@ __device__ __forceinline__ uint32_t h2_bits(__half lo16, __half hi16) {
 
 // ---------------------------------------------------------------- operands
 // Block = (job, group, 32 support vectors).  Writes the scaled C halves into
-// the B chunks and the packed j_s digits (digit t in byte t%4 of word t/4;
-// for q = 2 the digit is doubled so that the GEMM kernel works mod 4).
+// the B chunks and the group's table: the packed j_s digits (digit t in byte
+// t%4 of word t/4; for q = 2 the digit is doubled so that the GEMM kernel
+// works mod 4) after the (hi, lo) FP16 half2 words of omega^m.
 // FP32 throughout (GB300's FP64 rate is a small fraction of FP32): a_s is
 // FP32 already, the roots come from plan.roots, and the power-of-two scaling
 // is exact, so hi + lo carry C to FP32 accuracy.
@@ -184,8 +199,16 @@ __global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
     *reinterpret_cast<unsigned long long*>(reinterpret_cast<unsigned char*>(plan.gm_ws) + SCHED_OFF) = 0ull;
   const float sc = ldexpf(1.0f, 14 - ex);
 
+  // roots (KPS = 4: W = W_hi + W_lo), once per group
+  if (KPS == 4 && sb == 0 && tid < q) {
+    const float2 wq = sW[tid];
+    const __half hr = __float2half_rn(wq.x), hi = __float2half_rn(wq.y);
+    reinterpret_cast<uint2*>(rc)[tid] =
+        make_uint2(h2_bits(hr, hi), h2_bits(__float2half_rn(wq.x - __half2float(hr)),
+                                            __float2half_rn(wq.y - __half2float(hi))));
+  }
   // j table
-  uint32_t* jtab = reinterpret_cast<uint32_t*>(rc);
+  uint32_t* jtab = reinterpret_cast<uint32_t*>(rc + TAB_HDR);
   for (int e = tid; e < (s_hi - s_lo) * NW; e += blockDim.x) {
     const int sl = e / NW, wi = e % NW;
     uint32_t word = 0;
@@ -207,7 +230,7 @@ __global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
   auto dst = [&](int s, int h, int nn) {
     const int k0 = KPS * s;
     const int kc = k0 / KC, kin = k0 % KC;
-    return rc + g.jt_bytes + ((int64_t)h * g.nK + kc) * g.CB + sw128(nn, kin);
+    return rc + g.tab_bytes + ((int64_t)h * g.nK + kc) * g.CB + sw128(nn, kin);
   };
   auto put = [&](unsigned char* p, uint32_t v) {
     if (KPS == 2)
@@ -254,13 +277,13 @@ __global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
 // units of unequal cost balance by themselves.  Its load warp takes them and
 // publishes them in a small shared-memory queue; every role reads the same
 // sequence from it:
-//   producers  (MT*4 warps)  A chunks of the row block into a TMEM ring
-//   epilogue   (MT*4 warps)  accumulators -> U, one 32-row quarter of one tile each
-//   MMA warp                 tcgen05.mma into accumulator buffer (unit % nacc)
-//   load warp                B chunks (bulk copies) into a shared-memory ring
-// The A and B rings run on across unit boundaries, so the next unit's operands
-// are staged while the epilogue drains the last one; with two accumulator
-// buffers (nacc = 2) its MMAs also overlap that drain.
+//   producer set 0 (MT*4 warps)  K entries 0..31 of each A chunk into a TMEM ring
+//   producer set 1 (MT*4 warps)  K entries 32..63; then accumulators -> U, one
+//                                32-row quarter of one tile each
+//   MMA warp                     tcgen05.mma into accumulator buffer (unit % nacc)
+//   load warp                    units, tables and B chunks (bulk copies)
+// The A and B rings run on across unit boundaries, so set 0 and the load warp
+// stage the next unit's operands while set 1 drains the last one.
 constexpr int MAX_NB = 8;   // B stages (deeper: their bulk copies come from L2)
 constexpr int MAX_NA = 4;   // A stages
 constexpr int TMEM_COLS = 512;
@@ -273,19 +296,23 @@ __host__ __device__ inline int tmem_na(int mt, int nacc, int npmax) {
   return na > MAX_NA ? MAX_NA : na;
 }
 
+// A work unit as the load warp decodes it into the shared-memory queue (j < 0
+// ends the queue).  seq counts the CTA's units; its table goes to buffer seq % 2.
 struct Unit {
-  int j, c, h, q, b, S_pad, nK, NP, RP, rp0, nrp;
+  int j, c, h, q, b, S_pad, nK, NP, RP, rp0, nrp, seq;
   int64_t B, row0;
   const unsigned char* region;  // the job's region (header: inverse scale)
-  const uint32_t* gJ;           // the group's j table
+  const unsigned char* gT;      // the group's table (roots, j words)
   const unsigned char* gB;      // the chunk's B images
-  uint32_t CB;
+  uint32_t CB, TB;              // bytes of a B chunk, of the table copy
   float2* U;                    // samples of (job, group, first delay row of the chunk)
 };
+static_assert(sizeof(Unit) <= UNIT_BYTES, "unit queue entry");
 
 template <int KPS, int NW>
 __device__ __forceinline__ Unit decode_unit(const qsft_plan& plan, int64_t w, int nrows) {
   Unit x;
+  x.seq = 0;
   const int nj = plan.njobs;
   const int64_t* __restrict__ idx = plan.gm_index;
   x.j = find_job(idx, nj, w);
@@ -307,10 +334,11 @@ __device__ __forceinline__ Unit decode_unit(const qsft_plan& plan, int64_t w, in
   x.NP = g.NP;
   x.S_pad = g.S_pad;
   x.CB = g.CB;
+  x.TB = g.tab_copy;
   x.region = reinterpret_cast<const unsigned char*>(plan.gm_ws) + __ldg(idx + 2 * (nj + 1) + x.j);
   const unsigned char* gc = x.region + REGION_HDR + (int64_t)x.c * g.region_c;
-  x.gJ = reinterpret_cast<const uint32_t*>(gc);
-  x.gB = gc + g.jt_bytes + (int64_t)x.h * g.nK * g.CB;
+  x.gT = gc;
+  x.gB = gc + g.tab_bytes + (int64_t)x.h * g.nK * g.CB;
   x.U = reinterpret_cast<float2*>(plan.U) + job->off_U + ((int64_t)x.c * x.RP + x.rp0) * x.B;
   return x;
 }
@@ -334,29 +362,33 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
   // chunk g (counted over the CTA's whole unit range) uses A slot g % NA and B slot g % nb
   uint64_t* bfull = reinterpret_cast<uint64_t*>(smem);  // [MAX_NB] B chunk landed
   uint64_t* cons = bfull + MAX_NB;                      // [MAX_NB] every MMA of chunk g (at g % nb) completed
-  uint64_t* afull = cons + MAX_NB;                      // [MAX_NA] A chunk written
+  uint64_t* afull = cons + MAX_NB;                      // [MAX_NA] A chunk written (by both producer sets)
   uint64_t* accf = afull + MAX_NA;                      // [2] accumulator buffer written
   uint64_t* acce = accf + 2;                            // [2] accumulator buffer drained
   uint64_t* done = acce + 2;                            // every MMA issued has completed
-  uint64_t* uq_full = done + 1;                         // [UQ] unit index published
+  uint64_t* uq_full = done + 1;                         // [UQ] unit published
   uint64_t* uq_empty = uq_full + UQ;                    // [UQ] every consumer warp has read it
-  uint64_t* pbar = uq_empty + UQ;                       // producer warps' group barrier
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 384);
-  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 388);
-  volatile uint32_t* n_con = reinterpret_cast<volatile uint32_t*>(smem + 392);
-  uint2* qtab = reinterpret_cast<uint2*>(smem + 512);  // KPS = 4: (hi, lo) half2 words of omega^m
-  volatile long long* uq = reinterpret_cast<volatile long long*>(smem + 768);  // [UQ] unit indices, -1 ends
-  uint32_t* jt = reinterpret_cast<uint32_t*>(smem + HDR);
+  uint64_t* tfull = uq_empty + UQ;                      // [2] table buffer landed
+  uint64_t* tempty = tfull + 2;                         // [2] every producer warp is done with the table
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + 960);  // after the barriers
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + 964);
+  volatile uint32_t* n_con = reinterpret_cast<volatile uint32_t*>(smem + 968);
+  Unit* units = reinterpret_cast<Unit*>(smem + UNIT_OFF);  // [UQ] decoded units
+  unsigned char* tbuf = smem + HDR;                        // [2] table buffers of plan.gm_jt_bytes
   const int MT = plan.gm_mt, nacc = plan.gm_nacc, npmax = plan.gm_npmax;
+  const uint32_t TBB = (uint32_t)plan.gm_jt_bytes;
   // A slots: what tensor memory holds beside the accumulators, and fewer than the
   // B slots, so that a wait on cons[] for chunk g - NA cannot alias a later phase
   const int NA = min(tmem_na(MT, nacc, npmax), nb - 1);
   const uint32_t B_SLOT = (uint32_t)npmax * KC * 2;
-  unsigned char* bring = smem + HDR + plan.gm_jt_bytes;
+  unsigned char* bring = tbuf + 2 * TBB;
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nprod = MT * TM;
-  const int epi_warp0 = nprod / 32, mma_warp = 2 * nprod / 32, load_warp = mma_warp + 1;
+  // the MMA and load warps first: the warp schedulers favour lower warps, and the
+  // MMA warp's single thread must keep the tensor pipe fed beside the
+  // instruction-dense producer warps (warps 2.. : two sets of MT*4)
+  const int mma_warp = 0, load_warp = 1, prod_warp0 = 2;
 
   // ---- setup: accumulators at column buf*MT*npmax + t*npmax, then NA slots of MT A tiles
   const uint32_t acols = (uint32_t)(nacc * MT * npmax + 31) / 32 * 32;
@@ -370,19 +402,20 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
       mbar_init(&bfull[i], 1);
       mbar_init(&cons[i], 1);
     }
-    for (int i = 0; i < MAX_NA; ++i) mbar_init(&afull[i], MT * 4);
+    for (int i = 0; i < MAX_NA; ++i) mbar_init(&afull[i], 2 * MT * 4);  // both producer sets
     for (int i = 0; i < 2; ++i) {
       mbar_init(&accf[i], 1);
       mbar_init(&acce[i], MT * 4);
+      mbar_init(&tfull[i], 1);
+      mbar_init(&tempty[i], 2 * MT * 4);
     }
     mbar_init(done, 1);
     for (int i = 0; i < UQ; ++i) {
       mbar_init(&uq_full[i], 1);
-      mbar_init(&uq_empty[i], 2 * MT * 4 + 1);  // producer and epilogue warps, the MMA warp
+      mbar_init(&uq_empty[i], 2 * MT * 4 + 1);  // both producer sets, the MMA warp
     }
-    mbar_init(pbar, MT * 4);
     // the swizzled layout needs 1024-byte aligned atoms; the TMEM plan must fit
-    *abort_flag = ((smem_u32(bring) & 1023u) || NA < 2 || nb > MAX_NB || (MT != 1 && MT != 2) ||
+    *abort_flag = ((smem_u32(bring) & 1023u) || (TBB & 1023u) || NA < 2 || nb > MAX_NB || (MT != 1 && MT != 2) ||
                    (nacc != 1 && nacc != 2)) ? 1 : 0;
     *n_con = 0;
     fence_mbar_init();
@@ -391,66 +424,48 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
   __syncthreads();
   tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  uint32_t iss = 0;  // bulk copies issued (load warp, lane 0)
-  // next unit of a consumer warp (-1: no more, or a wait gave up); lane 0 takes
-  // it from the queue and frees the slot at once
-  auto next_unit = [&](Ring& r) -> long long {
-    long long u = -1;
+  uint32_t iss = 0, tl = 0;  // bulk copies of B chunks and of tables issued (load warp, lane 0)
+  // the next unit of a consumer warp, read by every lane from the queue (whose
+  // slot is freed at once); false when the queue has ended or a wait gave up
+  auto take_unit = [&](Ring& r, Unit& x) -> bool {
+    const int ok = __all_sync(~0u, mbar_wait(&uq_full[r.slot], r.phase) ? 1 : 0);
+    if (ok) x = units[r.slot];
+    __syncwarp();
     if (lane == 0) {
-      if (mbar_wait(&uq_full[r.slot], r.phase)) {
-        u = uq[r.slot];
-      } else {
-        *abort_flag = 1;
-      }
+      if (!ok) *abort_flag = 1;
       mbar_arrive(&uq_empty[r.slot]);
     }
     r.next();
-    return __shfl_sync(~0u, u, 0);
+    return ok && x.j >= 0;
   };
 
-  if (tid < nprod) {
-    // ---- producers: one row of A per thread, for every unit of the range
-    const int t = tid >> 7;
-    const uint32_t a_lane = tmem + ((uint32_t)(warp & 3) * 32 << 16) + acols + (uint32_t)t * A_COLS;
-    int cur_j = -1, cur_c = -1;
+  if (warp >= prod_warp0) {
+    // ---- producers, in two sets of MT*4 warps over the same rows: set 0
+    // writes K entries 0..31 of every chunk, set 1 entries 32..63, one row
+    // per thread; set 1 also reads each unit's accumulators back (the
+    // epilogue) once its MMAs have completed, and stores U
+    const int pw = warp - prod_warp0, set = pw / (MT * 4), wi = pw - set * MT * 4;
+    const int t = wi >> 2, lq = warp & 3;  // tile, lane quarter (warp % 4: the TMEM lanes this warp may access)
+    const int rr = t * TM + lq * 32 + lane;  // row within the unit
+    const uint32_t a_lane =
+        tmem + ((uint32_t)(lq * 32) << 16) + acols + (uint32_t)t * A_COLS + (uint32_t)set * (A_COLS / 2);
     Ring fa((uint32_t)NA);   // A slot of chunk g
     Ring ce((uint32_t)nb);   // cons[] position of chunk g - NA
-    Ring uqr(UQ);
-    uint32_t g = 0, pph = 0;
-    // the producer warps' group barrier (bounded): every producer thread's shared
-    // stores before it are visible to every producer thread after it
-    auto group_sync = [&]() {
-      __threadfence_block();
-      __syncwarp();
-      int ok = 1;
-      if (lane == 0) {
-        mbar_arrive(pbar);
-        ok = mbar_wait(pbar, pph);
-        if (!ok) *abort_flag = 1;
-      }
-      pph ^= 1;
-      __syncwarp();
-    };
-    for (;;) {
-      const long long u = next_unit(uqr);
-      if (u < 0) break;
-      const Unit x = decode_unit<KPS, NW>(plan, u, nprod);
-      if (x.j != cur_j || x.c != cur_c) {  // the group's j table (and q's roots) into shared memory
-        group_sync();                      // every producer is done with the previous table
-        for (int i = tid; i < x.S_pad * NW; i += nprod) jt[i] = __ldg(x.gJ + i);
-        if (KPS == 4 && tid < x.q) {
-          const double* r = plan.roots + ((int64_t)x.q * 32 + tid) * 2;
-          const float wr = (float)r[0], wi = (float)r[1];
-          const __half hr = __float2half_rn(wr), hi = __float2half_rn(wi);
-          qtab[tid] = make_uint2(h2_bits(hr, hi), h2_bits(__float2half_rn(wr - __half2float(hr)),
-                                                          __float2half_rn(wi - __half2float(hi))));
-        }
-        group_sync();
-        cur_j = x.j;
-        cur_c = x.c;
-      }
+    Ring ac((uint32_t)nacc), uqr(UQ);
+    uint32_t g = 0;
+    Unit x;
+    while (take_unit(uqr, x)) {
       if (*abort_flag) continue;  // keep taking units until the queue ends
-      const int64_t l = x.row0 + tid;
+      // the unit's table (every lane waits, so that the copied words are visible to it)
+      const uint32_t tk = (uint32_t)x.seq & 1u;
+      if (!__all_sync(~0u, mbar_wait(&tfull[tk], ((uint32_t)x.seq >> 1) & 1u) ? 1 : 0)) {
+        if (lane == 0) *abort_flag = 1;
+        continue;
+      }
+      const unsigned char* tab = tbuf + tk * TBB;
+      const uint2* qtab = reinterpret_cast<const uint2*>(tab);  // KPS = 4: (hi, lo) half2 words of omega^m
+      const uint32_t* jt = reinterpret_cast<const uint32_t*>(tab + TAB_HDR);
+      const int64_t l = x.row0 + rr;
       uint32_t lw[NW];
 #pragma unroll
       for (int k = 0; k < NW; ++k) lw[k] = 0;
@@ -466,15 +481,16 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
         }
       }
       const ModQ mq = make_modq(x.q);
-      // each chunk is computed before its slot is free (the wait overlaps the work)
+      bool ok = true;
+      // each half chunk is computed before its slot is free (the wait overlaps the work)
       for (int kc = 0; kc < x.nK; ++kc) {
-        const int s0 = kc * (KC / KPS);
-        uint32_t av[32];  // the row's 64 FP16 entries of this chunk, K order
+        const int s0 = kc * (KC / KPS) + set * (KC / 2 / KPS);
+        uint32_t av[16];  // the row's 32 FP16 entries of this half chunk, K order
         if constexpr (KPS == 2) {
           // four support vectors per 16-byte chunk; omega_4^m as half2 (re, im):
           // high bytes from the tables 0x00BC003C (re) and 0xBC003C00 (im), low bytes zero
 #pragma unroll
-          for (int i = 0; i < 8; ++i) {
+          for (int i = 0; i < 4; ++i) {
             const uint32_t* jp = jt + (s0 + 4 * i) * NW;
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
@@ -485,9 +501,9 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
             }
           }
         } else {
-          // two support vectors per chunk: (hi, lo) half2 words of omega^m
+          // two support vectors per 16-byte chunk: (hi, lo) half2 words of omega^m
 #pragma unroll
-          for (int i = 0; i < 8; ++i) {
+          for (int i = 0; i < 4; ++i) {
             const uint32_t* jp = jt + (s0 + 2 * i) * NW;
             uint32_t d0 = 0, d1 = 0;
 #pragma unroll
@@ -508,12 +524,13 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
           go = __shfl_sync(~0u, go, 0);
           if (!go) {
             if (lane == 0) *abort_flag = 1;
+            ok = false;
             break;
           }
           ce.next();
         }
         // store and signal at once: the MMA warp waits for this chunk, not for the next one's compute
-        tmem_st32(a_lane + fa.slot * (uint32_t)(MT * A_COLS), av);
+        tmem_st16(a_lane + fa.slot * (uint32_t)(MT * A_COLS), av);
         tmem_st_wait();
         tc_fence_before();
         __syncwarp();
@@ -521,30 +538,25 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
         fa.next();
         ++g;
       }
-    }
-  } else if (warp < mma_warp) {
-    // ---- epilogue: tile et, rows lq*32 + lane of it
-    const int et = (warp - epi_warp0) >> 2, lq = warp & 3;
-    Ring ac((uint32_t)nacc), uqr(UQ);
-    for (;;) {
-      const long long u = next_unit(uqr);
-      if (u < 0) break;
-      int ok = 1;
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[tk]);  // this warp is done with the table
+      if (set == 0 || !ok) continue;
+
+      // ---- epilogue (set 1): tile t, rows lq*32 + lane of it
+      const bool live = l < x.B;
+      float2* __restrict__ ur = x.U + l;
+      const float inv = *reinterpret_cast<const float*>(x.region);
+      int ready = 1;
       // one accumulator buffer: the MMA warp waits for this drain, so notice the
       // unit's end soon (128 ns cap); two: the drain overlaps MMAs, sleep longer
-      if (lane == 0) ok = !*abort_flag && mbar_wait_sleep(&accf[ac.slot], ac.phase, nacc == 1 ? 128u : 2048u);
-      ok = __shfl_sync(~0u, ok, 0);
-      if (!ok) {
+      if (lane == 0) ready = !*abort_flag && mbar_wait_sleep(&accf[ac.slot], ac.phase, nacc == 1 ? 128u : 2048u);
+      ready = __shfl_sync(~0u, ready, 0);
+      if (!ready) {
         if (lane == 0) *abort_flag = 1;
-        break;
+        continue;
       }
       tc_fence_after();
-      const Unit x = decode_unit<KPS, NW>(plan, u, nprod);
-      const int64_t row = x.row0 + et * TM + lq * 32 + lane;
-      const bool live = row < x.B;
-      const uint32_t tb = tmem + ((uint32_t)(lq * 32) << 16) + ac.slot * (uint32_t)(MT * npmax) + (uint32_t)(et * npmax);
-      float2* __restrict__ ur = x.U + row;
-      const float inv = *reinterpret_cast<const float*>(x.region);
+      const uint32_t tb = tmem + ((uint32_t)(lq * 32) << 16) + ac.slot * (uint32_t)(MT * npmax) + (uint32_t)(t * npmax);
       const int ng = x.NP / 16;
       const int nrp = x.nrp;
       const int64_t B = x.B;
@@ -580,27 +592,47 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
   } else if (warp == mma_warp) {
     // ---- MMA issue.  Descriptors differ between slots, tiles and K steps
     // only in the start-address field (smem address >> 4 < 2^14, no carry),
-    // so they are built once and offset.
+    // so they are built once and advanced by additions.  The loop is kept
+    // short: a thread needs ~50 cycles to issue one MMA, so every cycle it
+    // spends elsewhere can leave the tensor pipe without queued work.
     if (lane == 0) {
-      const uint64_t b0 = desc_sw128(smem_u32(bring));
+      const uint64_t b_first = desc_sw128(smem_u32(bring));
+      const uint32_t a_first = tmem + acols;
+      const uint32_t a_step = (uint32_t)(MT * A_COLS), b_step = B_SLOT >> 4;
       Ring fa((uint32_t)NA), fb((uint32_t)nb), ac((uint32_t)nacc), uqr(UQ);
+      uint32_t a_addr = a_first;  // A slot of chunk g
+      uint64_t b_desc = b_first;  // B slot of chunk g
       uint32_t g = 0;
+      // the four K = 16 steps of one tile (K = 16 is 32 bytes along the swizzled row)
+      auto tile_mmas = [&](uint32_t d, uint32_t a, uint64_t b, uint32_t idesc, uint32_t acc0) {
+        mma_f16_ts(d, a, b, idesc, acc0);
+        mma_f16_ts(d, a + 8, b + 2, idesc, 1u);
+        mma_f16_ts(d, a + 16, b + 4, idesc, 1u);
+        mma_f16_ts(d, a + 24, b + 6, idesc, 1u);
+      };
       for (;;) {
-        long long u = -1;  // lane 0 alone runs this loop: the queue without a shuffle
-        if (mbar_wait(&uq_full[uqr.slot], uqr.phase)) u = uq[uqr.slot]; else *abort_flag = 1;
+        // lane 0 alone runs this loop: the queue without the warp-wide take
+        int nK = 0, NP = 16, live = 0;
+        if (mbar_wait(&uq_full[uqr.slot], uqr.phase)) {
+          const Unit& s = units[uqr.slot];
+          live = s.j >= 0;
+          nK = s.nK;
+          NP = s.NP;
+        } else {
+          *abort_flag = 1;
+        }
         mbar_arrive(&uq_empty[uqr.slot]);
         uqr.next();
-        if (u < 0 || *abort_flag) break;
-        const Unit x = decode_unit<KPS, NW>(plan, u, nprod);
+        if (!live || *abort_flag) break;
         if (!mbar_wait(&acce[ac.slot], ac.phase ^ 1)) {
           *abort_flag = 1;
           break;
         }
         tc_fence_after();
-        const uint32_t idesc = tc::make_idesc(TM, x.NP);
-        const uint32_t dbase = tmem + ac.slot * (uint32_t)(MT * npmax);
+        const uint32_t idesc = tc::make_idesc(TM, NP);
+        const uint32_t d0 = tmem + ac.slot * (uint32_t)(MT * npmax), d1 = d0 + (uint32_t)npmax;
         bool ok = true;
-        for (int kc = 0; kc < x.nK; ++kc) {
+        for (int kc = 0; kc < nK; ++kc) {
           // both operands of chunk g: one non-blocking test each, issued together;
           // the bounded blocking waits only when either is not there yet
           const bool rb = mbar_test_wait(&bfull[fb.slot], fb.phase);
@@ -611,18 +643,24 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
             break;
           }
           tc_fence_after();
-          const uint32_t ad = tmem + acols + fa.slot * (uint32_t)(MT * A_COLS);
-          const uint64_t bd = b0 + ((fb.slot * B_SLOT) >> 4);
-          for (int t = 0; t < MT; ++t) {
-            const uint32_t dt = dbase + (uint32_t)(t * npmax);
-            const uint32_t at = ad + (uint32_t)(t * A_COLS);
-#pragma unroll
-            for (int ks = 0; ks < KC / 16; ++ks)  // K = 16 is 32 bytes along the swizzled row
-              mma_f16_ts(dt, at + ks * 8, bd + ks * 2, idesc, (kc | ks) > 0);
-          }
+          const uint32_t acc0 = kc > 0 ? 1u : 0u;
+          tile_mmas(d0, a_addr, b_desc, idesc, acc0);
+          if (MT == 2) tile_mmas(d1, a_addr + A_COLS, b_desc, idesc, acc0);
           mma_commit(&cons[fb.slot]);  // frees A slot and B slot of chunk g
-          fa.next();
-          fb.next();
+          if (++fa.slot == fa.n) {
+            fa.slot = 0;
+            fa.phase ^= 1;
+            a_addr = a_first;
+          } else {
+            a_addr += a_step;
+          }
+          if (++fb.slot == fb.n) {
+            fb.slot = 0;
+            fb.phase ^= 1;
+            b_desc = b_first;
+          } else {
+            b_desc += b_step;
+          }
           ++g;
         }
         if (!ok) {
@@ -638,40 +676,58 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
     }
     __syncwarp();
   } else if (warp == load_warp) {
-    // ---- B chunks: one bulk copy per slot, up to nb in flight, across units
+    // ---- scheduler and copies: takes units from the global counter (reset by
+    // the operand kernel), decodes each into the queue, then copies its table
+    // and streams its B chunks, one bulk copy per slot, up to nb in flight
     if (lane == 0) {
-      // also the scheduler: takes units from the global counter (reset by the
-      // operand kernel) and publishes them, one unit ahead of its own copies
       unsigned long long* counter =
           reinterpret_cast<unsigned long long*>(reinterpret_cast<unsigned char*>(plan.gm_ws) + SCHED_OFF);
       const long long total = plan.total_gm_work;
       Ring fb((uint32_t)nb), uqw(UQ);
       bool ended = false;
+      int seq = 0;
       // one unit per take: units of unequal cost balance by themselves and the
       // tail is a single unit (runs of consecutive units measured slower)
-      auto take = [&]() -> long long {
-        const long long u = (long long)atomicAdd(counter, 1ull);
-        return u < total ? u : -1;
-      };
-      auto publish = [&](bool stop) -> long long {
+      auto publish = [&](bool stop) -> int {  // queue slot of the unit published, -1 at the end
         if (ended) return -1;
         if (!mbar_wait(&uq_empty[uqw.slot], uqw.phase ^ 1)) {
           *abort_flag = 1;
           ended = true;
           return -1;
         }
-        const long long u = stop ? -1 : take();
-        uq[uqw.slot] = u;
-        mbar_arrive(&uq_full[uqw.slot]);  // release: the index is visible with the phase
+        long long u = -1;
+        if (!stop) {
+          u = (long long)atomicAdd(counter, 1ull);
+          if (u >= total) u = -1;
+        }
+        Unit* s = units + uqw.slot;
+        if (u >= 0) {
+          *s = decode_unit<KPS, NW>(plan, u, nprod);
+          s->seq = seq++;
+        } else {
+          s->j = -1;
+          ended = true;
+        }
+        mbar_arrive(&uq_full[uqw.slot]);  // release: the unit is visible with the phase
+        const int slot = (int)uqw.slot;
         uqw.next();
-        if (u < 0) ended = true;
-        return u;
+        return u >= 0 ? slot : -1;
       };
       uint32_t g = 0;
-      long long cur = publish(false);
-      long long ahead = cur >= 0 ? publish(false) : -1;
+      int cur = publish(false);
       while (cur >= 0) {
-        const Unit x = decode_unit<KPS, NW>(plan, cur, nprod);
+        const Unit x = units[cur];  // its slot is rewritten only UQ publications later
+        // the table into buffer seq % 2 once the producers are done with the
+        // unit two before (they are in the previous unit by now)
+        const uint32_t tk = (uint32_t)x.seq & 1u;
+        if (*abort_flag || (x.seq >= 2 && !mbar_wait(&tempty[tk], (((uint32_t)x.seq >> 1) - 1u) & 1u))) {
+          *abort_flag = 1;
+          break;
+        }
+        mbar_arrive_expect_tx(&tfull[tk], x.TB);
+        bulk_g2s(tbuf + tk * TBB, x.gT, x.TB, &tfull[tk]);
+        tl = (uint32_t)x.seq + 1;
+        const int nxt = publish(false);  // decoded while this unit's copies wait for slots
         for (int kc = 0; kc < x.nK; ++kc) {
           // slot reuse: the MMAs of chunk g - nb have completed (the first round passes)
           if (*abort_flag || !mbar_wait(&cons[fb.slot], fb.phase ^ 1)) {
@@ -684,17 +740,19 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
           iss = ++g;
         }
         if (*abort_flag) break;
-        cur = ahead;
-        ahead = cur >= 0 ? publish(false) : -1;
+        cur = nxt;
       }
       publish(true);  // ends the queue for every consumer (after an abort too)
     }
     __syncwarp();
   }
   __syncthreads();  // every role loop has ended; n_con is final
-  if (warp == load_warp && lane == 0)
+  if (warp == load_warp && lane == 0) {
     for (uint32_t k = *n_con; k < iss; ++k)  // copies that no MMA consumed: let them land (bounded)
       mbar_wait(&bfull[k % (uint32_t)nb], (k / (uint32_t)nb) & 1);
+    // the last table copy of each buffer (an earlier one was consumed before the buffer was reused)
+    for (uint32_t k = tl > 2 ? tl - 2 : 0; k < tl; ++k) mbar_wait(&tfull[k & 1u], (k >> 1) & 1u);
+  }
   tc_fence_before();
   __syncthreads();
   tc_fence_after();
@@ -702,9 +760,9 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
   if (warp == mma_warp) tmem_dealloc(tmem, ncols);
 }
 
-// B slots for the shared-memory budget (A lives in tensor memory)
+// B slots for the shared-memory budget (A lives in tensor memory; two table buffers)
 inline bool pick_stages(int npmax, int jt_bytes, int& nb, int& smem) {
-  const int fixed = HDR + jt_bytes, bb = npmax * KC * 2;
+  const int fixed = HDR + 2 * jt_bytes, bb = npmax * KC * 2;
   for (nb = MAX_NB; nb >= 3; --nb)  // at least 3: the A ring keeps 2 slots below it
     if (fixed + nb * bb <= MAX_SMEM) {
       smem = fixed + nb * bb;
@@ -768,17 +826,19 @@ extern "C" int qsft_gemm_layout(const qsft_job* jobs, int njobs, qsft_plan* plan
   }
   // tensor memory: nacc accumulator buffers of mt tiles + at least two A slots.
   // Preference: the larger mt (a B chunk feeds more rows, and the MMA warp's
-  // per-chunk waits and commit cover twice the MMAs), then two buffers (the
-  // epilogue overlaps the next unit's MMAs).  Presets cap both.
+  // per-chunk waits and commit cover twice the MMAs), then at least three A
+  // slots, then two buffers (the epilogue overlaps the next unit's MMAs).
+  // Presets cap mt and nacc.
   const int mt_cap = (plan->gm_mt == 1 || plan->gm_mt == 2) ? plan->gm_mt : 2;
   const int nacc_cap = plan->gm_nacc == 1 ? 1 : 2;
   int mt = 0, nacc = 0;
   for (int m = mt_cap; m >= 1 && !mt; --m)
-    for (int na_ = nacc_cap; na_ >= 1 && !mt; --na_)
-      if ((m == 1 || (int64_t)(m / 2) * gm::TM < maxB) && gm::tmem_na(m, na_, npmax) >= 2) {
-        mt = m;
-        nacc = na_;
-      }
+    for (int min_na = 3; min_na >= 2 && !mt; --min_na)
+      for (int na_ = nacc_cap; na_ >= 1 && !mt; --na_)
+        if ((m == 1 || (int64_t)(m / 2) * gm::TM < maxB) && gm::tmem_na(m, na_, npmax) >= min_na) {
+          mt = m;
+          nacc = na_;
+        }
   if (!mt) return QSFT_ERR_TOO_LARGE;
   int64_t work = 0, prep = 0, off = 0;
   index[0] = 0;
@@ -793,7 +853,7 @@ extern "C" int qsft_gemm_layout(const qsft_job* jobs, int njobs, qsft_plan* plan
     index[njobs + 2 + i] = prep;
     index[2 * (njobs + 1) + i] = off;
     off += gm::region_bytes(g, jb.C);
-    const int jtb = (g.S_pad * nw * 4 + 1023) / 1024 * 1024;  // keeps the rings 1024-byte aligned
+    const int jtb = gm::tab_smem(g);
     jt = jt > jtb ? jt : jtb;
   }
   int nb, smem;
