@@ -357,7 +357,7 @@ struct Ring {
 };
 
 template <int KPS, int NW>
-__global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan plan, int nb) {
+__global__ void __launch_bounds__(2 * 2 * TM + 96, 1) eval_gemm_kernel(qsft_plan plan, int nb) {
   extern __shared__ __align__(1024) unsigned char smem[];
   // chunk g (counted over the CTA's whole unit range) uses A slot g % NA and B slot g % nb
   uint64_t* bfull = reinterpret_cast<uint64_t*>(smem);  // [MAX_NB] B chunk landed
@@ -385,10 +385,11 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int nprod = MT * TM;
-  // the MMA and load warps first: the warp schedulers favour lower warps, and the
-  // MMA warp's single thread must keep the tensor pipe fed beside the
-  // instruction-dense producer warps (warps 2.. : two sets of MT*4)
-  const int mma_warp = 0, load_warp = 1, prod_warp0 = 2;
+  // warps 0 and 2 issue the MMAs of tiles 0 and 1 (one thread each: issuing
+  // an MMA takes a thread ~50 cycles, so one thread for both tiles left the
+  // tensor pipe waiting), warp 1 loads, warps 3.. are the two producer sets
+  const int mma_warp = 0, load_warp = 1, mma_warp2 = 2, prod_warp0 = 3;
+  const int n_mma = MT;  // MMA threads
 
   // ---- setup: accumulators at column buf*MT*npmax + t*npmax, then NA slots of MT A tiles
   const uint32_t acols = (uint32_t)(nacc * MT * npmax + 31) / 32 * 32;
@@ -400,19 +401,19 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
   if (tid == 0) {
     for (int i = 0; i < MAX_NB; ++i) {
       mbar_init(&bfull[i], 1);
-      mbar_init(&cons[i], 1);
+      mbar_init(&cons[i], n_mma);
     }
     for (int i = 0; i < MAX_NA; ++i) mbar_init(&afull[i], 2 * MT * 4);  // both producer sets
     for (int i = 0; i < 2; ++i) {
-      mbar_init(&accf[i], 1);
+      mbar_init(&accf[i], n_mma);
       mbar_init(&acce[i], MT * 4);
       mbar_init(&tfull[i], 1);
       mbar_init(&tempty[i], 2 * MT * 4);
     }
-    mbar_init(done, 1);
+    mbar_init(done, n_mma);
     for (int i = 0; i < UQ; ++i) {
       mbar_init(&uq_full[i], 1);
-      mbar_init(&uq_empty[i], 2 * MT * 4 + 1);  // both producer sets, the MMA warp
+      mbar_init(&uq_empty[i], 2 * MT * 4 + n_mma);  // both producer sets, the MMA threads
     }
     // the swizzled layout needs 1024-byte aligned atoms; the TMEM plan must fit
     *abort_flag = ((smem_u32(bring) & 1023u) || (TBB & 1023u) || NA < 2 || nb > MAX_NB || (MT != 1 && MT != 2) ||
@@ -589,15 +590,16 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
       if (lane == 0) mbar_arrive(&acce[ac.slot]);
       ac.next();
     }
-  } else if (warp == mma_warp) {
+  } else if (warp == mma_warp || (warp == mma_warp2 && MT == 2)) {
     // ---- MMA issue.  Descriptors differ between slots, tiles and K steps
     // only in the start-address field (smem address >> 4 < 2^14, no carry),
     // so they are built once and advanced by additions.  The loop is kept
     // short: a thread needs ~50 cycles to issue one MMA, so every cycle it
     // spends elsewhere can leave the tensor pipe without queued work.
     if (lane == 0) {
+      const uint32_t tile = warp == mma_warp ? 0u : 1u;  // this thread's tile
       const uint64_t b_first = desc_sw128(smem_u32(bring));
-      const uint32_t a_first = tmem + acols;
+      const uint32_t a_first = tmem + acols + tile * A_COLS;
       const uint32_t a_step = (uint32_t)(MT * A_COLS), b_step = B_SLOT >> 4;
       Ring fa((uint32_t)NA), fb((uint32_t)nb), ac((uint32_t)nacc), uqr(UQ);
       uint32_t a_addr = a_first;  // A slot of chunk g
@@ -630,7 +632,7 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
         }
         tc_fence_after();
         const uint32_t idesc = tc::make_idesc(TM, NP);
-        const uint32_t d0 = tmem + ac.slot * (uint32_t)(MT * npmax), d1 = d0 + (uint32_t)npmax;
+        const uint32_t d = tmem + ac.slot * (uint32_t)(MT * npmax) + tile * (uint32_t)npmax;
         bool ok = true;
         for (int kc = 0; kc < nK; ++kc) {
           // both operands of chunk g: one non-blocking test each, issued together;
@@ -643,10 +645,8 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
             break;
           }
           tc_fence_after();
-          const uint32_t acc0 = kc > 0 ? 1u : 0u;
-          tile_mmas(d0, a_addr, b_desc, idesc, acc0);
-          if (MT == 2) tile_mmas(d1, a_addr + A_COLS, b_desc, idesc, acc0);
-          mma_commit(&cons[fb.slot]);  // frees A slot and B slot of chunk g
+          tile_mmas(d, a_addr, b_desc, idesc, kc > 0 ? 1u : 0u);
+          mma_commit(&cons[fb.slot]);  // with the other tile's: frees A slot and B slot of chunk g
           if (++fa.slot == fa.n) {
             fa.slot = 0;
             fa.phase ^= 1;
@@ -667,10 +667,10 @@ __global__ void __launch_bounds__(2 * 2 * TM + 64, 1) eval_gemm_kernel(qsft_plan
           *abort_flag = 1;
           break;
         }
-        mma_commit(&accf[ac.slot]);  // arrives when every MMA of the unit has completed
+        mma_commit(&accf[ac.slot]);  // with the other tile's: every MMA of the unit has completed
         ac.next();
       }
-      *n_con = g;
+      atomicMax(const_cast<uint32_t*>(n_con), g);  // chunks whose B copy an MMA thread saw land
       mma_commit(done);  // arrives once every MMA issued above has completed
       if (!mbar_wait(done, 0)) *abort_flag = 1;
     }
@@ -785,7 +785,7 @@ static int launch(const qsft_plan* p, cudaStream_t st) {
   if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
     return QSFT_ERR_CUDA;
   const int64_t grid = p->total_gm_work < sms ? p->total_gm_work : sms;  // persistent: one CTA per SM
-  kern<<<(unsigned)grid, 2 * p->gm_mt * TM + 64, smem, st>>>(*p, nb);
+  kern<<<(unsigned)grid, 2 * p->gm_mt * TM + 96, smem, st>>>(*p, nb);
   QSFT_CUDA_CHECK_LAUNCH();
   return QSFT_OK;
 }
