@@ -246,6 +246,21 @@ __device__ __forceinline__ c2<T>* stage_col(const qsft_plan& plan, int jid, int 
   return reinterpret_cast<c2<T>*>(plan.stage) + (s0 + pos) * plan.stage_rp;
 }
 
+// Every phase deals the chunks of all jobs round-robin to the warps, so a warp
+// needs the item count of every job before its own.  The decode and peel
+// blocks load the counts of a window of jobs at once (-1 for a job that has
+// left the loop): a warp that walked the jobs reading each control record in
+// turn paid a dependent L2 round trip per job before it reached its work (the
+// scan keeps that walk: with the window it measured slower in later
+// iterations).
+constexpr int JOB_WIN = 256;
+template <class F>
+__device__ __forceinline__ void job_counts(int j0, int nj, int* s_cnt, F count) {
+  __syncthreads();  // the previous window's counts are read by every warp
+  for (int i = threadIdx.x; i < nj; i += blockDim.x) s_cnt[i] = count(j0 + i);
+  __syncthreads();
+}
+
 // A warp takes 32 bins at a time, a lane per bin: the first iteration every
 // bin (consecutive bins of a group: coalesced rows), later ones the bins the
 // previous iteration's subtractions changed.  Each bin's class is reset (the
@@ -335,213 +350,221 @@ __device__ __forceinline__ void decode_phase(const qsft_plan& plan) {
   const int ks = plan.kstride;
   c2<T>* sc = s_col[slot];
   uint8_t* kl = s_k[slot];
+  __shared__ int s_cnt[JOB_WIN];
   int64_t chunk0 = 0;
-  for (int jid = 0; jid < plan.njobs; ++jid) {
-    qsft_ctrl* ctl = plan.ctrl + jid;
-    if (ctl->done) continue;
-    const int cnt = ctl->n_cand;
-    const int nch = (cnt + DEC_CPW - 1) / DEC_CPW;
-    const int start = (int)(((int64_t)gw - chunk0) % nw + nw) % nw;
-    chunk0 += nch;
-    if (start >= nch) continue;
-    const qsft_job* __restrict__ job = plan.jobs + jid;
-    const int q = job->q, n = job->n, b = job->b, B = job->B, P = job->P, R = job->R;
-    const int RP = R * P, nsym = P - 1;
-    const double thr = job->cutoff * RP;
-    const bool staged = RP <= DEC_STAGE_RP;
-    const bool words_ok = (n & 3) == 0 && ((job->off_D & 3) == 0);
-    const float2* wq = s_w + q * 32;
-    uint8_t* syms = job->src == QSFT_SRC_CODED ? s_sym[slot] : kl;
-    const long long iter = (long long)ctl->iter + 1;
-    for (int ch = start; ch < nch; ch += nw) {   // uniform over the warp: every lane runs every sync
-      const int u = ch * DEC_CPW + lane / DEC_G;
-      const bool active = u < cnt;
-      const int local = active ? plan.cand[job->off_bin + u] : 0;
-      const int c = local / B, jb = local - (local / B) * B;
-      const int64_t gb = job->off_bin + local;
-      const c2<T>* col = reinterpret_cast<const c2<T>*>(plan.U) + job->off_U + (int64_t)c * RP * B + jb;
-      const c2<T>* stg = active ? stage_col<T>(plan, jid, u, RP) : nullptr;
-      if (staged && active) {
-        if (stg)
-          for (int r = gi; r < RP; r += DEC_G) sc[r] = stg[r];
-        else
-          for (int r = gi; r < RP; r += DEC_G) sc[r] = col[(int64_t)r * B];
-      }
-      __syncwarp();
-      auto V = [&](int r) -> c2<T> { return staged ? sc[r] : col[(int64_t)r * B]; };
-      // ---- channel decoding, symbols dealt over the group
-      if (active) {
-        if (job->chan == QSFT_CHAN_IDENTITY) {
-          const c2<T> v0 = V(0);
-          const T a0 = atan2(v0.y, v0.x);
-          for (int i = 1 + gi; i < RP && i <= nsym; i += DEC_G) {
-            const c2<T> vi = V(i);
-            const T ai = atan2(vi.y, vi.x);
-            double a = (double)((T)q * (ai - a0) / (T)6.283185307179586);
-            if (sizeof(T) == 4 && fabs(a - floor(a) - 0.5) < 1e-3)
-              a = (double)q * (atan2((double)vi.y, (double)vi.x) - atan2((double)v0.y, (double)v0.x)) /
-                  6.283185307179586;
-            long long m = (long long)rint(a);  // round half to even, like np.round
-            m %= q;
-            if (m < 0) m += q;
-            syms[i - 1] = (uint8_t)m;
-          }
-        } else {
-          for (int i = 1 + gi; i <= nsym; i += DEC_G) {
-            T zr = 0, zi = 0;
-            for (int r = 0; r < R; ++r) {
-              const c2<T> u0 = V(r * P), ui = V(r * P + i);
-              zr += u0.x * ui.x + u0.y * ui.y;
-              zi += u0.y * ui.x - u0.x * ui.y;
+  for (int j0 = 0; j0 < plan.njobs; j0 += JOB_WIN) {
+    const int nj = min(JOB_WIN, plan.njobs - j0);
+    job_counts(j0, nj, s_cnt, [&](int jid) -> int {
+      const qsft_ctrl* c = plan.ctrl + jid;
+      return __ldcg(&c->done) ? -1 : __ldcg(&c->n_cand);
+    });
+    for (int w = 0; w < nj; ++w) {
+      const int jid = j0 + w, cnt = s_cnt[w];
+      if (cnt < 0) continue;
+      qsft_ctrl* ctl = plan.ctrl + jid;
+      const int nch = (cnt + DEC_CPW - 1) / DEC_CPW;
+      const int start = (int)(((int64_t)gw - chunk0) % nw + nw) % nw;
+      chunk0 += nch;
+      if (start >= nch) continue;
+      const qsft_job* __restrict__ job = plan.jobs + jid;
+      const int q = job->q, n = job->n, b = job->b, B = job->B, P = job->P, R = job->R;
+      const int RP = R * P, nsym = P - 1;
+      const double thr = job->cutoff * RP;
+      const bool staged = RP <= DEC_STAGE_RP;
+      const bool words_ok = (n & 3) == 0 && ((job->off_D & 3) == 0);
+      const float2* wq = s_w + q * 32;
+      uint8_t* syms = job->src == QSFT_SRC_CODED ? s_sym[slot] : kl;
+      const long long iter = (long long)ctl->iter + 1;
+      for (int ch = start; ch < nch; ch += nw) {   // uniform over the warp: every lane runs every sync
+        const int u = ch * DEC_CPW + lane / DEC_G;
+        const bool active = u < cnt;
+        const int local = active ? plan.cand[job->off_bin + u] : 0;
+        const int c = local / B, jb = local - (local / B) * B;
+        const int64_t gb = job->off_bin + local;
+        const c2<T>* col = reinterpret_cast<const c2<T>*>(plan.U) + job->off_U + (int64_t)c * RP * B + jb;
+        const c2<T>* stg = active ? stage_col<T>(plan, jid, u, RP) : nullptr;
+        if (staged && active) {
+          if (stg)
+            for (int r = gi; r < RP; r += DEC_G) sc[r] = stg[r];
+          else
+            for (int r = gi; r < RP; r += DEC_G) sc[r] = col[(int64_t)r * B];
+        }
+        __syncwarp();
+        auto V = [&](int r) -> c2<T> { return staged ? sc[r] : col[(int64_t)r * B]; };
+        // ---- channel decoding, symbols dealt over the group
+        if (active) {
+          if (job->chan == QSFT_CHAN_IDENTITY) {
+            const c2<T> v0 = V(0);
+            const T a0 = atan2(v0.y, v0.x);
+            for (int i = 1 + gi; i < RP && i <= nsym; i += DEC_G) {
+              const c2<T> vi = V(i);
+              const T ai = atan2(vi.y, vi.x);
+              double a = (double)((T)q * (ai - a0) / (T)6.283185307179586);
+              if (sizeof(T) == 4 && fabs(a - floor(a) - 0.5) < 1e-3)
+                a = (double)q * (atan2((double)vi.y, (double)vi.x) - atan2((double)v0.y, (double)v0.x)) /
+                    6.283185307179586;
+              long long m = (long long)rint(a);  // round half to even, like np.round
+              m %= q;
+              if (m < 0) m += q;
+              syms[i - 1] = (uint8_t)m;
             }
-            if (sizeof(T) == 4) {
-              float ang = atan2f((float)zi, (float)zr);
-              if (ang < 0.f) ang += 6.28318530717958647f;
-              const float tq = ang * (float)q * 0.15915494309189535f;
-              if (fabsf(tq - floorf(tq) - 0.5f) >= 1e-3f) {
-                // away from a tie the nearest of 2 pi m / q, m = 0..q, is floor(tq + 1/2)
-                syms[i - 1] = (uint8_t)(((int)floorf(tq + 0.5f)) % q);
-                continue;
-              }
-              double dzr = 0, dzi = 0;  // near a rounding boundary: recompute in FP64
+          } else {
+            for (int i = 1 + gi; i <= nsym; i += DEC_G) {
+              T zr = 0, zi = 0;
               for (int r = 0; r < R; ++r) {
-                const double2 u0 = to_d2(V(r * P)), ui = to_d2(V(r * P + i));
-                dzr += u0.x * ui.x + u0.y * ui.y;
-                dzi += u0.y * ui.x - u0.x * ui.y;
+                const c2<T> u0 = V(r * P), ui = V(r * P + i);
+                zr += u0.x * ui.x + u0.y * ui.y;
+                zi += u0.y * ui.x - u0.x * ui.y;
               }
-              double ang64 = atan2(dzi, dzr);
-              if (ang64 < 0) ang64 += 6.283185307179586;
-              syms[i - 1] = (uint8_t)nearest_root(ang64, q);
-            } else {
-              double ang = (double)atan2(zi, zr);
-              if (ang < 0) ang += 6.283185307179586;
-              syms[i - 1] = (uint8_t)nearest_root(ang, q);
+              if (sizeof(T) == 4) {
+                float ang = atan2f((float)zi, (float)zr);
+                if (ang < 0.f) ang += 6.28318530717958647f;
+                const float tq = ang * (float)q * 0.15915494309189535f;
+                if (fabsf(tq - floorf(tq) - 0.5f) >= 1e-3f) {
+                  // away from a tie the nearest of 2 pi m / q, m = 0..q, is floor(tq + 1/2)
+                  syms[i - 1] = (uint8_t)(((int)floorf(tq + 0.5f)) % q);
+                  continue;
+                }
+                double dzr = 0, dzi = 0;  // near a rounding boundary: recompute in FP64
+                for (int r = 0; r < R; ++r) {
+                  const double2 u0 = to_d2(V(r * P)), ui = to_d2(V(r * P + i));
+                  dzr += u0.x * ui.x + u0.y * ui.y;
+                  dzi += u0.y * ui.x - u0.x * ui.y;
+                }
+                double ang64 = atan2(dzi, dzr);
+                if (ang64 < 0) ang64 += 6.283185307179586;
+                syms[i - 1] = (uint8_t)nearest_root(ang64, q);
+              } else {
+                double ang = (double)atan2(zi, zr);
+                if (ang < 0) ang += 6.283185307179586;
+                syms[i - 1] = (uint8_t)nearest_root(ang, q);
+              }
             }
           }
         }
-      }
-      __syncwarp();
-      // ---- source decoding
-      const bool coded = job->src == QSFT_SRC_CODED;
-      if (coded && active && gi == 0) {
-        const GFt g = make_gf(plan.gf_tables + job->rs_gf_off, q, job->rs_s);
-        rs_decode(g, q, job->rs_s, job->rs_t, n, syms, kl, kl + n);
-      }
-      __syncwarp();
-      for (int i = (coded ? 2 * n : n) + gi; i < ks; i += DEC_G) kl[i] = 0;
-      __syncwarp();
-      // ---- projection rho = <omega^(Dk), col> / RP and residual energy, rows
-      //      dealt over the group: FP32 for FP32 plans (FP64 within 1% of the
-      //      threshold), FP64 for FP64 plans
-      const int8_t* Dc = plan.i8 + job->off_D + (int64_t)c * RP * n;
-      auto project64 = [&](double2& rho_out, double& res_out) {
-        double ar = 0, ai = 0;
-        for (int r = gi; r < RP; r += DEC_G) {
-          const double2 w = root(plan.roots, q, row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q));
-          const double2 v = to_d2(V(r));
-          ar += w.x * v.x + w.y * v.y;
-          ai += w.x * v.y - w.y * v.x;
+        __syncwarp();
+        // ---- source decoding
+        const bool coded = job->src == QSFT_SRC_CODED;
+        if (coded && active && gi == 0) {
+          const GFt g = make_gf(plan.gf_tables + job->rs_gf_off, q, job->rs_s);
+          rs_decode(g, q, job->rs_s, job->rs_t, n, syms, kl, kl + n);
         }
-        ar = group_sum(ar, gmask);
-        ai = group_sum(ai, gmask);
-        const double2 rh = make_double2(ar / RP, ai / RP);
-        double rs = 0;
-        for (int r = gi; r < RP; r += DEC_G) {
-          const double2 w = root(plan.roots, q, row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q));
-          const double2 v = to_d2(V(r));
-          const double dx = v.x - (rh.x * w.x - rh.y * w.y);
-          const double dy = v.y - (rh.x * w.y + rh.y * w.x);
-          rs += dx * dx + dy * dy;
-        }
-        rho_out = rh;
-        res_out = group_sum(rs, gmask);
-      };
-      double2 rho = make_double2(0.0, 0.0);
-      double res = 0.0;
-      if (sizeof(T) == 4) {
-        int ph[(DEC_STAGE_RP + DEC_G - 1) / DEC_G];
-        float ar = 0.f, ai = 0.f;
-#pragma unroll
-        for (int k = 0; k < (DEC_STAGE_RP + DEC_G - 1) / DEC_G; ++k) {
-          const int r = gi + k * DEC_G;
-          ph[k] = 0;
-          if (r < RP) {
-            ph[k] = row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q);
-            const float2 w = wq[ph[k]];
+        __syncwarp();
+        for (int i = (coded ? 2 * n : n) + gi; i < ks; i += DEC_G) kl[i] = 0;
+        __syncwarp();
+        // ---- projection rho = <omega^(Dk), col> / RP and residual energy, rows
+        //      dealt over the group: FP32 for FP32 plans (FP64 within 1% of the
+        //      threshold), FP64 for FP64 plans
+        const int8_t* Dc = plan.i8 + job->off_D + (int64_t)c * RP * n;
+        auto project64 = [&](double2& rho_out, double& res_out) {
+          double ar = 0, ai = 0;
+          for (int r = gi; r < RP; r += DEC_G) {
+            const double2 w = root(plan.roots, q, row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q));
+            const double2 v = to_d2(V(r));
+            ar += w.x * v.x + w.y * v.y;
+            ai += w.x * v.y - w.y * v.x;
+          }
+          ar = group_sum(ar, gmask);
+          ai = group_sum(ai, gmask);
+          const double2 rh = make_double2(ar / RP, ai / RP);
+          double rs = 0;
+          for (int r = gi; r < RP; r += DEC_G) {
+            const double2 w = root(plan.roots, q, row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q));
+            const double2 v = to_d2(V(r));
+            const double dx = v.x - (rh.x * w.x - rh.y * w.y);
+            const double dy = v.y - (rh.x * w.y + rh.y * w.x);
+            rs += dx * dx + dy * dy;
+          }
+          rho_out = rh;
+          res_out = group_sum(rs, gmask);
+        };
+        double2 rho = make_double2(0.0, 0.0);
+        double res = 0.0;
+        if (sizeof(T) == 4) {
+          int ph[(DEC_STAGE_RP + DEC_G - 1) / DEC_G];
+          float ar = 0.f, ai = 0.f;
+  #pragma unroll
+          for (int k = 0; k < (DEC_STAGE_RP + DEC_G - 1) / DEC_G; ++k) {
+            const int r = gi + k * DEC_G;
+            ph[k] = 0;
+            if (r < RP) {
+              ph[k] = row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q);
+              const float2 w = wq[ph[k]];
+              const c2<T> v = V(r);
+              ar += w.x * (float)v.x + w.y * (float)v.y;
+              ai += w.x * (float)v.y - w.y * (float)v.x;
+            }
+          }
+          for (int r = gi + DEC_STAGE_RP; r < RP; r += DEC_G) {  // rows past the register-held phases
+            const float2 w = wq[row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q)];
             const c2<T> v = V(r);
             ar += w.x * (float)v.x + w.y * (float)v.y;
             ai += w.x * (float)v.y - w.y * (float)v.x;
           }
-        }
-        for (int r = gi + DEC_STAGE_RP; r < RP; r += DEC_G) {  // rows past the register-held phases
-          const float2 w = wq[row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q)];
-          const c2<T> v = V(r);
-          ar += w.x * (float)v.x + w.y * (float)v.y;
-          ai += w.x * (float)v.y - w.y * (float)v.x;
-        }
-        ar = group_sum(ar, gmask) / (float)RP;
-        ai = group_sum(ai, gmask) / (float)RP;
-        float rs = 0.f;
-#pragma unroll
-        for (int k = 0; k < (DEC_STAGE_RP + DEC_G - 1) / DEC_G; ++k) {
-          const int r = gi + k * DEC_G;
-          if (r < RP) {
-            const float2 w = wq[ph[k]];
+          ar = group_sum(ar, gmask) / (float)RP;
+          ai = group_sum(ai, gmask) / (float)RP;
+          float rs = 0.f;
+  #pragma unroll
+          for (int k = 0; k < (DEC_STAGE_RP + DEC_G - 1) / DEC_G; ++k) {
+            const int r = gi + k * DEC_G;
+            if (r < RP) {
+              const float2 w = wq[ph[k]];
+              const c2<T> v = V(r);
+              const float dx = (float)v.x - (ar * w.x - ai * w.y);
+              const float dy = (float)v.y - (ar * w.y + ai * w.x);
+              rs += dx * dx + dy * dy;
+            }
+          }
+          for (int r = gi + DEC_STAGE_RP; r < RP; r += DEC_G) {
+            const float2 w = wq[row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q)];
             const c2<T> v = V(r);
             const float dx = (float)v.x - (ar * w.x - ai * w.y);
             const float dy = (float)v.y - (ar * w.y + ai * w.x);
             rs += dx * dx + dy * dy;
           }
+          rs = group_sum(rs, gmask);
+          rho = make_double2(ar, ai);
+          res = rs;
+          if (fabsf(rs - (float)thr) <= 1e-2f * (float)thr) project64(rho, res);  // group-uniform
+        } else {
+          project64(rho, res);
         }
-        for (int r = gi + DEC_STAGE_RP; r < RP; r += DEC_G) {
-          const float2 w = wq[row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q)];
-          const c2<T> v = V(r);
-          const float dx = (float)v.x - (ar * w.x - ai * w.y);
-          const float dy = (float)v.y - (ar * w.y + ai * w.x);
-          rs += dx * dx + dy * dy;
+        // ---- bin match: digit t of M_c^T k equals digit t of j (MSB first), digits over the group
+        bool ok = true;
+        {
+          const int8_t* Mc = plan.i8 + job->off_M + (int64_t)c * n * b;
+          for (int t = gi; t < b; t += DEC_G) {
+            int jr = jb;
+            for (int tt = b - 1; tt > t; --tt) jr /= q;
+            int dg = 0;
+            for (int i = 0; i < n; ++i) dg += (int)Mc[i * b + t] * (int)kl[i];
+            ok &= (dg % q) == (jr % q);
+          }
         }
-        rs = group_sum(rs, gmask);
-        rho = make_double2(ar, ai);
-        res = rs;
-        if (fabsf(rs - (float)thr) <= 1e-2f * (float)thr) project64(rho, res);  // group-uniform
-      } else {
-        project64(rho, res);
+        const bool match = (__ballot_sync(0xffffffffu, !ok) & gmask) == 0;
+        const bool single = match && !(res > thr);
+        bool firstb = false;
+        int bid = -1;
+        if (active && gi == 0) {
+          plan.bin_status[gb] = single ? 2 : 1;
+          if (single) {
+            plan.rho[2 * gb] = rho.x;   // the peel reads the coefficient of the ball's last bin
+            plan.rho[2 * gb + 1] = rho.y;
+            bid = record_one(plan, job, ctl, kl, local, rho, iter, ks, firstb);
+          }
+        }
+        {  // the class counts, one atomic per warp and counter
+          const unsigned ns = __ballot_sync(0xffffffffu, active && gi == 0 && single);
+          const unsigned nm = __ballot_sync(0xffffffffu, active && gi == 0 && !single);
+          if (lane == 0) {
+            if (ns) atomicAdd(&ctl->n_single, __popc(ns));
+            if (nm) atomicAdd(&ctl->n_multi, __popc(nm));
+          }
+        }
+        const int pos = warp_append(firstb, jid, &ctl->n_unique);   // the iteration's list of balls
+        if (firstb) plan.uniq[job->off_ball + pos] = bid;
+        __syncwarp();  // the slot's buffers are reused by the next bin
       }
-      // ---- bin match: digit t of M_c^T k equals digit t of j (MSB first), digits over the group
-      bool ok = true;
-      {
-        const int8_t* Mc = plan.i8 + job->off_M + (int64_t)c * n * b;
-        for (int t = gi; t < b; t += DEC_G) {
-          int jr = jb;
-          for (int tt = b - 1; tt > t; --tt) jr /= q;
-          int dg = 0;
-          for (int i = 0; i < n; ++i) dg += (int)Mc[i * b + t] * (int)kl[i];
-          ok &= (dg % q) == (jr % q);
-        }
-      }
-      const bool match = (__ballot_sync(0xffffffffu, !ok) & gmask) == 0;
-      const bool single = match && !(res > thr);
-      bool firstb = false;
-      int bid = -1;
-      if (active && gi == 0) {
-        plan.bin_status[gb] = single ? 2 : 1;
-        if (single) {
-          plan.rho[2 * gb] = rho.x;   // the peel reads the coefficient of the ball's last bin
-          plan.rho[2 * gb + 1] = rho.y;
-          bid = record_one(plan, job, ctl, kl, local, rho, iter, ks, firstb);
-        }
-      }
-      {  // the class counts, one atomic per warp and counter
-        const unsigned ns = __ballot_sync(0xffffffffu, active && gi == 0 && single);
-        const unsigned nm = __ballot_sync(0xffffffffu, active && gi == 0 && !single);
-        if (lane == 0) {
-          if (ns) atomicAdd(&ctl->n_single, __popc(ns));
-          if (nm) atomicAdd(&ctl->n_multi, __popc(nm));
-        }
-      }
-      const int pos = warp_append(firstb, jid, &ctl->n_unique);   // the iteration's list of balls
-      if (firstb) plan.uniq[job->off_ball + pos] = bid;
-      __syncwarp();  // the slot's buffers are reused by the next bin
     }
   }
 }
@@ -602,111 +625,119 @@ __device__ __forceinline__ void peel_phase(const qsft_plan& plan) {
   const int lane = threadIdx.x & 31;
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
   const int ks = plan.kstride;
+  __shared__ int s_cnt[JOB_WIN];
   int64_t chunk0 = 0;
-  for (int jid = 0; jid < plan.njobs; ++jid) {
-    qsft_ctrl* ctl = plan.ctrl + jid;
-    if (ctl->done) continue;
-    const qsft_job* __restrict__ job = plan.jobs + jid;
-    const int C = job->C;
-    const int cnt = ctl->n_unique * C;
-    const int G = cnt >= PEEL_THREAD_MIN ? 1 : DEC_G, cpw = 32 / G, gi = lane % G;
-    if (G > 1 && !have_w && cnt > 0) {  // uniform over the block: every thread sees the same counts
-      for (int i = threadIdx.x; i < 33 * 32; i += blockDim.x)
-        s_w[i] = make_float2((float)plan.roots[2 * i], (float)plan.roots[2 * i + 1]);
-      __syncthreads();
-      have_w = true;
-    }
-    const unsigned gmask = ((1u << G) - 1) << (lane - gi);
-    const int nch = (cnt + cpw - 1) / cpw;
-    const int start = (int)(((int64_t)gw - chunk0) % nw + nw) % nw;
-    chunk0 += nch;
-    if (start >= nch) continue;
-    const int q = job->q, n = job->n, b = job->b, B = job->B;
-    const int RP = job->R * job->P;
-    const int iter = ctl->iter + 1;
-    const int parity = iter & 1;
-    const bool words_ok = (n & 3) == 0 && ((job->off_D & 3) == 0);
-    const float2* wq = s_w + q * 32;
-    int32_t* list = plan.dirty + (int64_t)parity * plan.total_bins + job->off_bin;
-    for (int ch = start; ch < nch; ch += nw) {   // uniform over the warp
-      const int it = ch * cpw + lane / G;
-      bool fresh = false;
-      int lb = 0;
-      if (G == 1) {
-        if (it < cnt) {
-          const int u = it / C, l = it - (it / C) * C;
-          const int bid = __ldcg(plan.uniq + job->off_ball + u);
-          const int64_t gball = job->off_ball + bid;
-          const unsigned long long best = __ldcg(reinterpret_cast<const unsigned long long*>(plan.ball_best) + gball);
-          const int64_t gbest = job->off_bin + (int64_t)(best & 0xffffffffull);
-          const double2 rho = make_double2(__ldcg(plan.rho + 2 * gbest), __ldcg(plan.rho + 2 * gbest + 1));
-          const uint8_t* kl = plan.ball_k + gball * ks;  // written by the record kernel
-          const int8_t* Ml = plan.i8 + job->off_M + (int64_t)l * n * b;
-          int jl = 0;
-          for (int t = 0; t < b; ++t) {  // bin index, MSB-first digits of M_l^T k
-            int dg = 0;
-            for (int i = 0; i < n; ++i) dg += (int)Ml[i * b + t] * (int)kl[i];
-            jl = jl * q + dg % q;
-          }
-          c2<T>* Ul = reinterpret_cast<c2<T>*>(plan.U) + job->off_U + (int64_t)l * RP * B + jl;
-          const int8_t* Dl = plan.i8 + job->off_D + (int64_t)l * RP * n;
-          if (sizeof(T) == 4) {
-            const float rx = (float)rho.x, ry = (float)rho.y;
-            for (int r = 0; r < RP; ++r) {
-              const double2 w = root(plan.roots, q, row_phase(Dl + (int64_t)r * n, kl, n, words_ok, q));
-              const float wx = (float)w.x, wy = (float)w.y;
-              sub_entry(Ul + (int64_t)r * B, rx * wx - ry * wy, rx * wy + ry * wx);
-            }
-          } else {
-            for (int r = 0; r < RP; ++r) {
-              const double2 w = root(plan.roots, q, row_phase(Dl + (int64_t)r * n, kl, n, words_ok, q));
-              sub_entry(Ul + (int64_t)r * B, rho.x * w.x - rho.y * w.y, rho.x * w.y + rho.y * w.x);
-            }
-          }
-          lb = l * B + jl;
-          fresh = atomicExch(plan.bin_stamp + job->off_bin + lb, iter) != iter;
-        }
-      } else {
-        const bool active = it < cnt;
-        const int u = active ? it / C : 0, l = active ? it - (it / C) * C : 0;
-        const int bid = active ? __ldcg(plan.uniq + job->off_ball + u) : 0;
-        const int64_t gball = job->off_ball + bid;
-        const uint8_t* kl = plan.ball_k + gball * ks;
-        const int8_t* Ml = plan.i8 + job->off_M + (int64_t)l * n * b;
-        int part = 0;  // this thread's digits of the bin index
-        if (active)
-          for (int t = gi; t < b; t += G) {
-            int dg = 0;
-            for (int i = 0; i < n; ++i) dg += (int)Ml[i * b + t] * (int)kl[i];
-            int pw = 1;
-            for (int tt = t + 1; tt < b; ++tt) pw *= q;
-            part += (dg % q) * pw;
-          }
-        const int jl = group_sum_g(part, gmask, G);
-        if (active) {
-          const unsigned long long best = __ldcg(reinterpret_cast<const unsigned long long*>(plan.ball_best) + gball);
-          const int64_t gbest = job->off_bin + (int64_t)(best & 0xffffffffull);
-          const double2 rho = make_double2(__ldcg(plan.rho + 2 * gbest), __ldcg(plan.rho + 2 * gbest + 1));
-          c2<T>* Ul = reinterpret_cast<c2<T>*>(plan.U) + job->off_U + (int64_t)l * RP * B + jl;
-          const int8_t* Dl = plan.i8 + job->off_D + (int64_t)l * RP * n;
-          if (sizeof(T) == 4) {
-            const float rx = (float)rho.x, ry = (float)rho.y;
-            for (int r = gi; r < RP; r += G) {
-              const float2 w = wq[row_phase(Dl + (int64_t)r * n, kl, n, words_ok, q)];
-              sub_entry(Ul + (int64_t)r * B, rx * w.x - ry * w.y, rx * w.y + ry * w.x);
-            }
-          } else {
-            for (int r = gi; r < RP; r += G) {
-              const double2 w = root(plan.roots, q, row_phase(Dl + (int64_t)r * n, kl, n, words_ok, q));
-              sub_entry(Ul + (int64_t)r * B, rho.x * w.x - rho.y * w.y, rho.x * w.y + rho.y * w.x);
-            }
-          }
-          lb = l * B + jl;
-          if (gi == 0) fresh = atomicExch(plan.bin_stamp + job->off_bin + lb, iter) != iter;
-        }
+  for (int j0 = 0; j0 < plan.njobs; j0 += JOB_WIN) {
+    const int nj = min(JOB_WIN, plan.njobs - j0);
+    job_counts(j0, nj, s_cnt, [&](int jid) -> int {
+      const qsft_ctrl* c = plan.ctrl + jid;
+      return __ldcg(&c->done) ? -1 : __ldcg(&c->n_unique) * __ldg(&plan.jobs[jid].C);
+    });
+    for (int w = 0; w < nj; ++w) {
+      const int jid = j0 + w, cnt = s_cnt[w];
+      if (cnt < 0) continue;
+      qsft_ctrl* ctl = plan.ctrl + jid;
+      const qsft_job* __restrict__ job = plan.jobs + jid;
+      const int C = job->C;
+      const int G = cnt >= PEEL_THREAD_MIN ? 1 : DEC_G, cpw = 32 / G, gi = lane % G;
+      if (G > 1 && !have_w && cnt > 0) {  // uniform over the block: every thread sees the same counts
+        for (int i = threadIdx.x; i < 33 * 32; i += blockDim.x)
+          s_w[i] = make_float2((float)plan.roots[2 * i], (float)plan.roots[2 * i + 1]);
+        __syncthreads();
+        have_w = true;
       }
-      const int pos = warp_append(fresh, jid, &ctl->n_dirty[parity]);  // once per bin per iteration
-      if (fresh) list[pos] = lb;
+      const unsigned gmask = ((1u << G) - 1) << (lane - gi);
+      const int nch = (cnt + cpw - 1) / cpw;
+      const int start = (int)(((int64_t)gw - chunk0) % nw + nw) % nw;
+      chunk0 += nch;
+      if (start >= nch) continue;
+      const int q = job->q, n = job->n, b = job->b, B = job->B;
+      const int RP = job->R * job->P;
+      const int iter = ctl->iter + 1;
+      const int parity = iter & 1;
+      const bool words_ok = (n & 3) == 0 && ((job->off_D & 3) == 0);
+      const float2* wq = s_w + q * 32;
+      int32_t* list = plan.dirty + (int64_t)parity * plan.total_bins + job->off_bin;
+      for (int ch = start; ch < nch; ch += nw) {   // uniform over the warp
+        const int it = ch * cpw + lane / G;
+        bool fresh = false;
+        int lb = 0;
+        if (G == 1) {
+          if (it < cnt) {
+            const int u = it / C, l = it - (it / C) * C;
+            const int bid = __ldcg(plan.uniq + job->off_ball + u);
+            const int64_t gball = job->off_ball + bid;
+            const unsigned long long best = __ldcg(reinterpret_cast<const unsigned long long*>(plan.ball_best) + gball);
+            const int64_t gbest = job->off_bin + (int64_t)(best & 0xffffffffull);
+            const double2 rho = make_double2(__ldcg(plan.rho + 2 * gbest), __ldcg(plan.rho + 2 * gbest + 1));
+            const uint8_t* kl = plan.ball_k + gball * ks;  // written by the record kernel
+            const int8_t* Ml = plan.i8 + job->off_M + (int64_t)l * n * b;
+            int jl = 0;
+            for (int t = 0; t < b; ++t) {  // bin index, MSB-first digits of M_l^T k
+              int dg = 0;
+              for (int i = 0; i < n; ++i) dg += (int)Ml[i * b + t] * (int)kl[i];
+              jl = jl * q + dg % q;
+            }
+            c2<T>* Ul = reinterpret_cast<c2<T>*>(plan.U) + job->off_U + (int64_t)l * RP * B + jl;
+            const int8_t* Dl = plan.i8 + job->off_D + (int64_t)l * RP * n;
+            if (sizeof(T) == 4) {
+              const float rx = (float)rho.x, ry = (float)rho.y;
+              for (int r = 0; r < RP; ++r) {
+                const double2 w = root(plan.roots, q, row_phase(Dl + (int64_t)r * n, kl, n, words_ok, q));
+                const float wx = (float)w.x, wy = (float)w.y;
+                sub_entry(Ul + (int64_t)r * B, rx * wx - ry * wy, rx * wy + ry * wx);
+              }
+            } else {
+              for (int r = 0; r < RP; ++r) {
+                const double2 w = root(plan.roots, q, row_phase(Dl + (int64_t)r * n, kl, n, words_ok, q));
+                sub_entry(Ul + (int64_t)r * B, rho.x * w.x - rho.y * w.y, rho.x * w.y + rho.y * w.x);
+              }
+            }
+            lb = l * B + jl;
+            fresh = atomicExch(plan.bin_stamp + job->off_bin + lb, iter) != iter;
+          }
+        } else {
+          const bool active = it < cnt;
+          const int u = active ? it / C : 0, l = active ? it - (it / C) * C : 0;
+          const int bid = active ? __ldcg(plan.uniq + job->off_ball + u) : 0;
+          const int64_t gball = job->off_ball + bid;
+          const uint8_t* kl = plan.ball_k + gball * ks;
+          const int8_t* Ml = plan.i8 + job->off_M + (int64_t)l * n * b;
+          int part = 0;  // this thread's digits of the bin index
+          if (active)
+            for (int t = gi; t < b; t += G) {
+              int dg = 0;
+              for (int i = 0; i < n; ++i) dg += (int)Ml[i * b + t] * (int)kl[i];
+              int pw = 1;
+              for (int tt = t + 1; tt < b; ++tt) pw *= q;
+              part += (dg % q) * pw;
+            }
+          const int jl = group_sum_g(part, gmask, G);
+          if (active) {
+            const unsigned long long best = __ldcg(reinterpret_cast<const unsigned long long*>(plan.ball_best) + gball);
+            const int64_t gbest = job->off_bin + (int64_t)(best & 0xffffffffull);
+            const double2 rho = make_double2(__ldcg(plan.rho + 2 * gbest), __ldcg(plan.rho + 2 * gbest + 1));
+            c2<T>* Ul = reinterpret_cast<c2<T>*>(plan.U) + job->off_U + (int64_t)l * RP * B + jl;
+            const int8_t* Dl = plan.i8 + job->off_D + (int64_t)l * RP * n;
+            if (sizeof(T) == 4) {
+              const float rx = (float)rho.x, ry = (float)rho.y;
+              for (int r = gi; r < RP; r += G) {
+                const float2 w = wq[row_phase(Dl + (int64_t)r * n, kl, n, words_ok, q)];
+                sub_entry(Ul + (int64_t)r * B, rx * w.x - ry * w.y, rx * w.y + ry * w.x);
+              }
+            } else {
+              for (int r = gi; r < RP; r += G) {
+                const double2 w = root(plan.roots, q, row_phase(Dl + (int64_t)r * n, kl, n, words_ok, q));
+                sub_entry(Ul + (int64_t)r * B, rho.x * w.x - rho.y * w.y, rho.x * w.y + rho.y * w.x);
+              }
+            }
+            lb = l * B + jl;
+            if (gi == 0) fresh = atomicExch(plan.bin_stamp + job->off_bin + lb, iter) != iter;
+          }
+        }
+        const int pos = warp_append(fresh, jid, &ctl->n_dirty[parity]);  // once per bin per iteration
+        if (fresh) list[pos] = lb;
+      }
     }
   }
 }
