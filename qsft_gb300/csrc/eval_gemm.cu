@@ -238,8 +238,12 @@ __global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
     else
       *reinterpret_cast<uint2*>(p) = make_uint2(v, v);
   };
-  for (int e = tid; e < (s_hi - s_lo) * RP; e += blockDim.x) {
-    const int sl = e / RP, rp = e % RP, s = s_lo + sl;
+  // items (delay row, support vector), support vector fastest: a warp writes
+  // 32 consecutive words of each B row (one 128-byte swizzled row), not one
+  // word of 32 rows
+  const int ns = s_hi - s_lo;
+  for (int e = tid; e < ns * RP; e += blockDim.x) {
+    const int rp = e / ns, sl = e - rp * ns, s = s_lo + sl;
     const int h = rp / g.RPC, nb = 4 * (rp - h * g.RPC);
     uint32_t rh = 0, rl = 0, ih = 0, il = 0;
     if (sl < s_live) {
@@ -266,8 +270,8 @@ __global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
   // padding columns of every chunk (the last chunk may hold fewer delay rows)
   for (int h = 0; h < g.nch; ++h) {
     const int rows = min(g.RPC, RP - h * g.RPC), npad = g.NP - 4 * rows;
-    for (int e = tid; e < (s_hi - s_lo) * npad; e += blockDim.x)
-      put(dst(s_lo + e / npad, h, 4 * rows + e % npad), 0u);
+    for (int e = tid; e < ns * npad; e += blockDim.x)
+      put(dst(s_lo + e % ns, h, 4 * rows + e / ns), 0u);
   }
 }
 
