@@ -248,7 +248,7 @@ def pin_summary(recs):
 # DRAM bytes per launch from one ncu capture of this workload (dram__bytes_read.sum +
 # dram__bytes_write.sum; profiles/eval_gemm_q4n20b7_batch16.md for the GEMM kernel, an
 # earlier capture for its operand kernel, profiles/gwht_rowc_q4n20b7_batch16.md)
-NCU_TRAFFIC = {"eval": (35.07e6 + 202.97e6) + (12.94e6 + 12.53e6), "gwht": 264.32e6 + 203.06e6, "batch": 16}
+NCU_TRAFFIC = {"eval": (35.07e6 + 203.15e6) + (12.94e6 + 12.53e6), "gwht": 264.32e6 + 203.06e6, "batch": 16}
 
 
 def run_reference(args):
