@@ -12,9 +12,9 @@ result collection.  Every batch holds > 129 MB of bins, so successive steps
 stream from HBM rather than L2.
 
   value  transforms/s with inputs resident on the device (CUDA events); the
-         steps alternate between two captured workspaces on two streams, so
-         two batches are in flight as in e2e (the serial replay of one
-         workspace on one stream is reported beside it)
+         steps go round four captured workspaces on four streams, so four
+         batches are in flight as in e2e (the serial replay of one workspace
+         on one stream is reported beside it)
   e2e    transforms/s through qsft_gb300.serve.transform_batch with host
          inputs, host->device copies of those inputs and the device->host read
          of every result inside the timed region (wall clock + sync)
@@ -422,15 +422,19 @@ def run_ours(args):
                 acc[k] += ev[k][0].elapsed_time(ev[k][1])
 
     batch.capture()                         # one CUDA graph per step
-    # a second workspace with the same inputs: the timed steps alternate between
-    # the two on two streams, two batches in flight as in the end-to-end run
-    batch2 = Batch([r.spec() for r in reqs], precision=args.precision, device=dev, peel_mode=args.peel_mode)
-    batch2.capture()
-    streams = (torch.cuda.Stream(dev), torch.cuda.Stream(dev))
-    pair = (batch, batch2)
+    # three more workspaces with the same inputs: the timed steps go round the
+    # four on four streams, four batches in flight as in the end-to-end run
+    # (ms per step, same box: one in flight 1.163, two 1.005, three 0.996, four 0.983)
+    NW = 4
+    ring = [batch]
+    for _ in range(NW - 1):
+        bx = Batch([r.spec() for r in reqs], precision=args.precision, device=dev, peel_mode=args.peel_mode)
+        bx.capture()
+        ring.append(bx)
+    streams = [torch.cuda.Stream(dev) for _ in range(NW)]
     for _ in range(max(args.warmup, 3)):
-        batch.run()
-        batch2.run()
+        for bx in ring:
+            bx.run()
     barrier()
     # clocks: sampled every 50 ms from an untimed ~0.4 s run of the same step
     # just before the timed steps until their end (the K timed steps alone are
@@ -450,19 +454,19 @@ def run_ours(args):
     t1e.record(stream)
     barrier()
     serial_ms = max_over_ranks(t0e.elapsed_time(t1e))
-    # the headline: steps alternate between the two workspaces on two streams
-    # (step i waits for step i-2 on its own stream only), CUDA events from a
-    # start event both streams wait on to the later of their end events
-    t0e, ends = torch.cuda.Event(enable_timing=True), [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    # the headline: steps go round the workspaces on their streams (step i
+    # waits for step i-NW on its own stream only), CUDA events from a start
+    # event every stream waits on to the latest of their end events
+    t0e, ends = torch.cuda.Event(enable_timing=True), [torch.cuda.Event(enable_timing=True) for _ in range(NW)]
     t0e.record(stream)
     for s in streams:
         s.wait_event(t0e)
     for i in range(args.steps):
-        pair[i % 2].run(streams[i % 2])
+        ring[i % NW].run(streams[i % NW])
     for e, s in zip(ends, streams):
         e.record(s)
     barrier()
-    launches = sum(pair[i % 2].launches_per_run() for i in range(args.steps))   # library kernels the replays ran
+    launches = sum(ring[i % NW].launches_per_run() for i in range(args.steps))   # library kernels the replays ran
     dev_ms = max(t0e.elapsed_time(e) for e in ends)
     clocks = clk.stop()
     dev_ms = max_over_ranks(dev_ms)
@@ -481,12 +485,14 @@ def run_ours(args):
     # pipelines the steps (host packing / parsing of one batch overlaps the
     # GPU's work on the next); every step still packs and uploads its inputs
     # and reads back its results inside the timed region
-    # a ring of three workspaces, two batches in flight: the host's packing and
-    # parsing of one batch hides behind the GPU's work on the next two
+    # a ring of five workspaces, four batches in flight: the host's packing and
+    # parsing of one batch hides behind the GPU's work on the next four (ms
+    # per batch, same box: two in flight 1.18, three 1.10, four 1.08)
     from collections import deque
-    ts = TransformStream(precision=args.precision, depth=3)
+    AHEAD = 4
+    ts = TransformStream(precision=args.precision, depth=AHEAD + 1)
     for _ in range(max(args.warmup, 3)):
-        tks = [ts.submit(reqs) for _ in range(3)]
+        tks = [ts.submit(reqs) for _ in range(AHEAD + 1)]
         for tk in tks:
             ts.result(tk)
     barrier()
@@ -495,7 +501,7 @@ def run_ours(args):
     inflight = deque()
     for i in range(args.steps):
         inflight.append(ts.submit(reqs))
-        if len(inflight) > 2:
+        if len(inflight) > AHEAD:
             ts.result(inflight.popleft())
     while inflight:
         ts.result(inflight.popleft())
@@ -607,8 +613,8 @@ def run_ours(args):
         "config": {"workload": "q4_n20_b7_C3_nso_R2_S1000_10dB", **WORKLOAD, "batch": J,
                    "parallelism": f"replicas x{world}", "peel_mode": args.peel_mode, "l2": "inputs > L2 (bins %.0f MB/step)" %
                    (samples * 8 * J / 1e6)},
-        "value_note": "inputs resident on the device; steps alternate between two captured workspaces on two "
-                      "streams (two batches in flight, the overlap e2e also has)",
+        "value_note": "inputs resident on the device; steps go round four captured workspaces on four "
+                      "streams (four batches in flight, as in e2e)",
         "value_serial_replay": J * args.steps * world / (serial_ms / 1e3),
         "latency_ms": {"p50": float(np.percentile(lat, 50) * 1e3), "p99": float(np.percentile(lat, 99) * 1e3),
                        "note": "batch completion latency through transform_batch"},
