@@ -206,6 +206,13 @@ class Batch:
         self.kstride = ks_.value
         self.jobs_host = jobs
         self.n_i8, self.n_a, self.n_u = off_i8, off_a, off_u
+        # the padding after each job's M, D and K rows (zeros), so that `load`
+        # writes the whole digit buffer with one concatenation
+        self._pads = []
+        for jb, sp in zip(jobs, specs):
+            ends = (jb.off_M + sp.M.size, jb.off_D + sp.D.size, jb.off_K + (0 if sp.K is None else sp.K.size))
+            nxt = (jb.off_D, jb.off_K, (ends[2] + 15) & ~15)
+            self._pads.append([np.zeros(b - a, np.int8) for a, b in zip(ends, nxt)])
         self.eval_prefix_host = eval_prefix
         self.gf_host = np.concatenate(gf_parts) if gf_parts else np.zeros(1, np.int32)
         self.njobs = J
@@ -419,18 +426,22 @@ class Batch:
         jobs = self.jobs_host
         i8 = self.i8_host.numpy()
         a = self.A_host.numpy()
+        pieces, apieces = [], []
+        empty = np.zeros(0, np.int8)
         for j, sp in enumerate(specs):
             jb = jobs[j]
             jb.max_iter = sp.max_iter
             jb.cutoff = sp.cutoff
             jb.noise_nu = sp.noise_nu
             jb.noise_seed = sp.noise_seed
-            i8[jb.off_M:jb.off_M + sp.M.size] = sp.M.ravel()
-            i8[jb.off_D:jb.off_D + sp.D.size] = sp.D.ravel()
-            if sp.K is not None:
-                i8[jb.off_K:jb.off_K + sp.K.size] = sp.K.ravel()
+            pm, pd, pk = self._pads[j]
+            pieces += [sp.M.ravel(), pm, sp.D.ravel(), pd, empty if sp.K is None else sp.K.ravel(), pk]
             if sp.A is not None:
-                a[jb.off_A:jb.off_A + sp.A.size] = sp.A
+                apieces.append(sp.A.ravel())
+        if self.n_i8:
+            np.concatenate(pieces, out=i8[:self.n_i8], casting="same_kind")
+        if apieces:
+            np.concatenate(apieces, out=a[:self.n_a], casting="same_kind")
         self.jobs_host_t.numpy()[:] = np.frombuffer(bytes(jobs), dtype=np.uint8)
         st = stream if stream is not None else torch.cuda.current_stream(self.device)
         with torch.cuda.stream(st):
@@ -641,17 +652,26 @@ class Batch:
         vals = out_val[:rows * 2].reshape(-1, 2)
         cnts = out_cnt[:rows]
         self.d2h_bytes = self.meta.numel() * 8 + rows * (self.kstride + 16 + 4)
+        # every row converted at once (copies: the buffers may be staging memory
+        # that the next read-back overwrites), then a view per job
+        v_all = vals.view(np.complex128).reshape(-1).copy()
+        c_all = cnts.copy()
+        n0 = self.shapes[0][1]
+        same_n = not any(self.coded) and all(sh[1] == n0 for sh in self.shapes)
+        k_all = ks[:, :n0].astype(np.int64) if same_n else None
         out = []
         for j, shape in enumerate(self.shapes):
             if ctrls[j].err:
                 raise _lib.QsftError(f"job {j}: device table overflow during peeling")
             s, c = int(idx[j, 0]), int(idx[j, 1])
             n = shape[1]
-            keys = ks[s:s + c, :n].astype(np.int64)
-            if self.coded[j]:
-                keys += shape[0] * ks[s:s + c, n:2 * n].astype(np.int64)
-            v = vals[s:s + c, 0] + 1j * vals[s:s + c, 1]
-            out.append((keys, v, cnts[s:s + c].copy(), ctrls[j]))
+            if same_n:
+                keys = k_all[s:s + c]
+            else:
+                keys = ks[s:s + c, :n].astype(np.int64)
+                if self.coded[j]:
+                    keys += shape[0] * ks[s:s + c, n:2 * n].astype(np.int64)
+            out.append((keys, v_all[s:s + c], c_all[s:s + c], ctrls[j]))
         return out
 
     def device_status(self):
