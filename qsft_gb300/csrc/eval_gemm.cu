@@ -288,7 +288,11 @@ __global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
 //   load warp                    units, tables and B chunks (bulk copies)
 // The A and B rings run on across unit boundaries, so set 0 and the load warp
 // stage the next unit's operands while set 1 drains the last one.
-constexpr int MAX_NB = 8;   // B stages (deeper: their bulk copies come from L2)
+// B stages.  Four: the bulk copies are off the critical path (skipping them
+// changed nothing), and the smaller shared-memory footprint (110 KB instead of
+// 200 KB per CTA) measured 4% faster per step with four batches in flight
+// (1% slower for one batch alone)
+constexpr int MAX_NB = 4;
 constexpr int MAX_NA = 4;   // A stages
 constexpr int TMEM_COLS = 512;
 constexpr int UQ = 8;       // queue of work units shared by the roles
