@@ -143,25 +143,25 @@ __device__ __forceinline__ bool krow_eq(const uint8_t* mine, const uint8_t* othe
   return eq;
 }
 
-// A candidate bin is decoded by a group of DEC_G threads (DEC_G consecutive
-// lanes; a warp holds 32 / DEC_G bins): symbols, rows and digits are dealt
+// A candidate bin is decoded by a group of G threads (G consecutive lanes; a
+// warp holds 32 / G bins; G = 8 in the first iteration, 16 later, when there
+// are fewer candidates to overlap): symbols, rows and digits are dealt
 // over the group and its sums reduced with in-group shuffles, so the dependent
 // chain of one bin stays short.  A warp works on bins of one job (chunks dealt
 // round-robin), so control flow is uniform.  The column's RP values (stride B
 // in U) are staged in shared memory with one round of loads when
 // RP <= DEC_STAGE_RP; FP32 roots for every q come from a block-wide table.
 constexpr int DEC_THREADS = 128;
-constexpr int DEC_G = 8;
-constexpr int DEC_CPW = 32 / DEC_G;                    // bins per warp at a time
-constexpr int DEC_BINS = DEC_THREADS / DEC_G;          // bins per block at a time
+constexpr int DEC_G = 8;        // lanes per candidate in the first iteration (and the persistent loop)
+constexpr int DEC_G_LATER = 16; // in later iterations: fewer candidates, more lanes on each
 constexpr int DEC_STAGE_RP = 64;
 constexpr int DEC_KB = 2 * QSFT_MAX_N;   // k row: n digits mod q, then n high parts for a coded source
 constexpr int PEEL_THREAD_MIN = 1024;  // peel items of a job at least this many: one thread per item
 
-template <typename V>
+template <int G, typename V>
 __device__ __forceinline__ V group_sum(V v, unsigned mask) {
 #pragma unroll
-  for (int o = DEC_G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+  for (int o = G / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
   return v;
 }
 // the same over groups of g (a power of two <= 32) lanes, g chosen at run time
@@ -332,10 +332,10 @@ __global__ void __launch_bounds__(SCAN_THREADS, sizeof(T) == 4 ? 4 : 3) scan_ker
 // iteration appended to the iteration's list.
 constexpr int DEC_BLOCKS = 152 * 5;   // resident at once (5 blocks of 128 threads per SM)
 
-// blocks of NT threads (NT / DEC_G bin slots)
-template <typename T, int NT>
+// blocks of NT threads (NT / G bin slots), groups of G lanes per candidate
+template <typename T, int NT, int G>
 __device__ __forceinline__ void decode_phase(const qsft_plan& plan) {
-  constexpr int NB = NT / DEC_G;
+  constexpr int NB = NT / G;
   __shared__ float2 s_w[33 * 32];                            // roots, FP32
   __shared__ c2<T> s_col[NB][DEC_STAGE_RP];
   __shared__ __align__(16) uint8_t s_k[NB][DEC_KB];
@@ -343,9 +343,9 @@ __device__ __forceinline__ void decode_phase(const qsft_plan& plan) {
   for (int i = threadIdx.x; i < 33 * 32; i += blockDim.x)
     s_w[i] = make_float2((float)plan.roots[2 * i], (float)plan.roots[2 * i + 1]);
   __syncthreads();
-  const int lane = threadIdx.x & 31, gi = lane % DEC_G;
-  const int slot = threadIdx.x / DEC_G;                      // the block's bin slot of this group
-  const unsigned gmask = ((1u << DEC_G) - 1) << (lane - gi);
+  const int lane = threadIdx.x & 31, gi = lane % G;
+  const int slot = threadIdx.x / G;                      // the block's bin slot of this group
+  const unsigned gmask = ((1u << G) - 1) << (lane - gi);
   const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
   const int ks = plan.kstride;
   c2<T>* sc = s_col[slot];
@@ -362,7 +362,7 @@ __device__ __forceinline__ void decode_phase(const qsft_plan& plan) {
       const int jid = j0 + w, cnt = s_cnt[w];
       if (cnt < 0) continue;
       qsft_ctrl* ctl = plan.ctrl + jid;
-      const int nch = (cnt + DEC_CPW - 1) / DEC_CPW;
+      const int nch = (cnt + (32 / G) - 1) / (32 / G);
       const int start = (int)(((int64_t)gw - chunk0) % nw + nw) % nw;
       chunk0 += nch;
       if (start >= nch) continue;
@@ -376,7 +376,7 @@ __device__ __forceinline__ void decode_phase(const qsft_plan& plan) {
       uint8_t* syms = job->src == QSFT_SRC_CODED ? s_sym[slot] : kl;
       const long long iter = (long long)ctl->iter + 1;
       for (int ch = start; ch < nch; ch += nw) {   // uniform over the warp: every lane runs every sync
-        const int u = ch * DEC_CPW + lane / DEC_G;
+        const int u = ch * (32 / G) + lane / G;
         const bool active = u < cnt;
         const int local = active ? plan.cand[job->off_bin + u] : 0;
         const int c = local / B, jb = local - (local / B) * B;
@@ -385,9 +385,9 @@ __device__ __forceinline__ void decode_phase(const qsft_plan& plan) {
         const c2<T>* stg = active ? stage_col<T>(plan, jid, u, RP) : nullptr;
         if (staged && active) {
           if (stg)
-            for (int r = gi; r < RP; r += DEC_G) sc[r] = stg[r];
+            for (int r = gi; r < RP; r += G) sc[r] = stg[r];
           else
-            for (int r = gi; r < RP; r += DEC_G) sc[r] = col[(int64_t)r * B];
+            for (int r = gi; r < RP; r += G) sc[r] = col[(int64_t)r * B];
         }
         __syncwarp();
         auto V = [&](int r) -> c2<T> { return staged ? sc[r] : col[(int64_t)r * B]; };
@@ -396,7 +396,7 @@ __device__ __forceinline__ void decode_phase(const qsft_plan& plan) {
           if (job->chan == QSFT_CHAN_IDENTITY) {
             const c2<T> v0 = V(0);
             const T a0 = atan2(v0.y, v0.x);
-            for (int i = 1 + gi; i < RP && i <= nsym; i += DEC_G) {
+            for (int i = 1 + gi; i < RP && i <= nsym; i += G) {
               const c2<T> vi = V(i);
               const T ai = atan2(vi.y, vi.x);
               double a = (double)((T)q * (ai - a0) / (T)6.283185307179586);
@@ -409,7 +409,7 @@ __device__ __forceinline__ void decode_phase(const qsft_plan& plan) {
               syms[i - 1] = (uint8_t)m;
             }
           } else {
-            for (int i = 1 + gi; i <= nsym; i += DEC_G) {
+            for (int i = 1 + gi; i <= nsym; i += G) {
               T zr = 0, zi = 0;
               for (int r = 0; r < R; ++r) {
                 const c2<T> u0 = V(r * P), ui = V(r * P + i);
@@ -450,7 +450,7 @@ __device__ __forceinline__ void decode_phase(const qsft_plan& plan) {
           rs_decode(g, q, job->rs_s, job->rs_t, n, syms, kl, kl + n);
         }
         __syncwarp();
-        for (int i = (coded ? 2 * n : n) + gi; i < ks; i += DEC_G) kl[i] = 0;
+        for (int i = (coded ? 2 * n : n) + gi; i < ks; i += G) kl[i] = 0;
         __syncwarp();
         // ---- projection rho = <omega^(Dk), col> / RP and residual energy, rows
         //      dealt over the group: FP32 for FP32 plans (FP64 within 1% of the
@@ -458,17 +458,17 @@ __device__ __forceinline__ void decode_phase(const qsft_plan& plan) {
         const int8_t* Dc = plan.i8 + job->off_D + (int64_t)c * RP * n;
         auto project64 = [&](double2& rho_out, double& res_out) {
           double ar = 0, ai = 0;
-          for (int r = gi; r < RP; r += DEC_G) {
+          for (int r = gi; r < RP; r += G) {
             const double2 w = root(plan.roots, q, row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q));
             const double2 v = to_d2(V(r));
             ar += w.x * v.x + w.y * v.y;
             ai += w.x * v.y - w.y * v.x;
           }
-          ar = group_sum(ar, gmask);
-          ai = group_sum(ai, gmask);
+          ar = group_sum<G>(ar, gmask);
+          ai = group_sum<G>(ai, gmask);
           const double2 rh = make_double2(ar / RP, ai / RP);
           double rs = 0;
-          for (int r = gi; r < RP; r += DEC_G) {
+          for (int r = gi; r < RP; r += G) {
             const double2 w = root(plan.roots, q, row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q));
             const double2 v = to_d2(V(r));
             const double dx = v.x - (rh.x * w.x - rh.y * w.y);
@@ -476,16 +476,16 @@ __device__ __forceinline__ void decode_phase(const qsft_plan& plan) {
             rs += dx * dx + dy * dy;
           }
           rho_out = rh;
-          res_out = group_sum(rs, gmask);
+          res_out = group_sum<G>(rs, gmask);
         };
         double2 rho = make_double2(0.0, 0.0);
         double res = 0.0;
         if (sizeof(T) == 4) {
-          int ph[(DEC_STAGE_RP + DEC_G - 1) / DEC_G];
+          int ph[(DEC_STAGE_RP + G - 1) / G];
           float ar = 0.f, ai = 0.f;
   #pragma unroll
-          for (int k = 0; k < (DEC_STAGE_RP + DEC_G - 1) / DEC_G; ++k) {
-            const int r = gi + k * DEC_G;
+          for (int k = 0; k < (DEC_STAGE_RP + G - 1) / G; ++k) {
+            const int r = gi + k * G;
             ph[k] = 0;
             if (r < RP) {
               ph[k] = row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q);
@@ -495,18 +495,18 @@ __device__ __forceinline__ void decode_phase(const qsft_plan& plan) {
               ai += w.x * (float)v.y - w.y * (float)v.x;
             }
           }
-          for (int r = gi + DEC_STAGE_RP; r < RP; r += DEC_G) {  // rows past the register-held phases
+          for (int r = gi + DEC_STAGE_RP; r < RP; r += G) {  // rows past the register-held phases
             const float2 w = wq[row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q)];
             const c2<T> v = V(r);
             ar += w.x * (float)v.x + w.y * (float)v.y;
             ai += w.x * (float)v.y - w.y * (float)v.x;
           }
-          ar = group_sum(ar, gmask) / (float)RP;
-          ai = group_sum(ai, gmask) / (float)RP;
+          ar = group_sum<G>(ar, gmask) / (float)RP;
+          ai = group_sum<G>(ai, gmask) / (float)RP;
           float rs = 0.f;
   #pragma unroll
-          for (int k = 0; k < (DEC_STAGE_RP + DEC_G - 1) / DEC_G; ++k) {
-            const int r = gi + k * DEC_G;
+          for (int k = 0; k < (DEC_STAGE_RP + G - 1) / G; ++k) {
+            const int r = gi + k * G;
             if (r < RP) {
               const float2 w = wq[ph[k]];
               const c2<T> v = V(r);
@@ -515,14 +515,14 @@ __device__ __forceinline__ void decode_phase(const qsft_plan& plan) {
               rs += dx * dx + dy * dy;
             }
           }
-          for (int r = gi + DEC_STAGE_RP; r < RP; r += DEC_G) {
+          for (int r = gi + DEC_STAGE_RP; r < RP; r += G) {
             const float2 w = wq[row_phase(Dc + (int64_t)r * n, kl, n, words_ok, q)];
             const c2<T> v = V(r);
             const float dx = (float)v.x - (ar * w.x - ai * w.y);
             const float dy = (float)v.y - (ar * w.y + ai * w.x);
             rs += dx * dx + dy * dy;
           }
-          rs = group_sum(rs, gmask);
+          rs = group_sum<G>(rs, gmask);
           rho = make_double2(ar, ai);
           res = rs;
           if (fabsf(rs - (float)thr) <= 1e-2f * (float)thr) project64(rho, res);  // group-uniform
@@ -533,7 +533,7 @@ __device__ __forceinline__ void decode_phase(const qsft_plan& plan) {
         bool ok = true;
         {
           const int8_t* Mc = plan.i8 + job->off_M + (int64_t)c * n * b;
-          for (int t = gi; t < b; t += DEC_G) {
+          for (int t = gi; t < b; t += G) {
             int jr = jb;
             for (int tt = b - 1; tt > t; --tt) jr /= q;
             int dg = 0;
@@ -569,11 +569,11 @@ __device__ __forceinline__ void decode_phase(const qsft_plan& plan) {
   }
 }
 
-template <typename T>
+template <typename T, int G>
 // FP32: 5 blocks per SM (up to 102 registers)
 __global__ void __launch_bounds__(DEC_THREADS, sizeof(T) == 4 ? 5 : 4) decode_kernel(qsft_plan plan) {
   if (__ldcg(plan.done_count) >= plan.njobs) return;  // every job has left the loop
-  decode_phase<T, DEC_THREADS>(plan);
+  decode_phase<T, DEC_THREADS, G>(plan);
 }
 
 // ---------------------------------------------------------------- peel
@@ -824,7 +824,7 @@ __global__ void __launch_bounds__(LOOP_THREADS, 4) peel_loop_kernel(qsft_plan pl
     if (__ldcg(plan.done_count) >= plan.njobs) break;  // the same in every block: read after a barrier
     scan_phase<T>(plan, it == 0);
     if (!grid_barrier(plan, expected)) return;
-    decode_phase<T, LOOP_THREADS>(plan);
+    decode_phase<T, LOOP_THREADS, DEC_G>(plan);
     if (!grid_barrier(plan, expected)) return;
     peel_phase<T>(plan);
     if (!grid_barrier(plan, expected)) return;
@@ -871,7 +871,13 @@ static int iteration(const qsft_plan* plan, int first, cudaStream_t st, cudaGrap
                      int set_cond = 0, int max_iter = 0) {
   scan_kernel<T><<<SCAN_BLOCKS, SCAN_THREADS, 0, st>>>(*plan, first);
   QSFT_CUDA_CHECK_LAUNCH();
-  decode_kernel<T><<<DEC_BLOCKS, DEC_THREADS, 0, st>>>(*plan);
+  // groups of 8 lanes for the first iteration's many candidates, of 16 for the
+  // later iterations' few (ms, 16 transforms: iteration 1 0.119 with 8, 0.140
+  // with 16; iteration 2 0.055 with 8, 0.042 with 16)
+  if (first)
+    decode_kernel<T, DEC_G><<<DEC_BLOCKS, DEC_THREADS, 0, st>>>(*plan);
+  else
+    decode_kernel<T, DEC_G_LATER><<<DEC_BLOCKS, DEC_THREADS, 0, st>>>(*plan);
   QSFT_CUDA_CHECK_LAUNCH();
   peel_kernel<T><<<LIST_BLOCKS, PEEL_THREADS, 0, st>>>(*plan, cond, set_cond, max_iter);
   QSFT_CUDA_CHECK_LAUNCH();
@@ -891,7 +897,7 @@ static int add_body(const qsft_plan* plan, cudaGraph_t body, cudaGraphConditiona
     unsigned grid, block;
     void** args;
   } ks[] = {{(void*)scan_kernel<T>, SCAN_BLOCKS, SCAN_THREADS, a0},
-            {(void*)decode_kernel<T>, DEC_BLOCKS, DEC_THREADS, a1},
+            {(void*)decode_kernel<T, DEC_G_LATER>, DEC_BLOCKS, DEC_THREADS, a1},
             {(void*)peel_kernel<T>, LIST_BLOCKS, PEEL_THREADS, a2}};
   cudaGraphNode_t prev = nullptr;
   for (const K& k : ks) {
