@@ -49,7 +49,7 @@
 // into a shared-memory queue, each with its group's table of j_s digits and
 // FP16 roots copied into one of two table buffers).  A chunk takes a producer
 // about as long as its MMAs take the tensor pipe, so one set alone (the
-// epilogue warps idle between drains) left the MMA warp waiting for A.
+// epilogue warps idle between drains) left the MMA threads waiting for A.
 // mbarriers: afull (both producer sets wrote an A chunk) / bfull (bulk copy
 // landed), one "chunk consumed" barrier per B slot that frees both rings (one
 // commit per chunk), accf (a unit's MMAs completed) / acce (its accumulators
@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(256) gemm_prep_kernel(qsft_plan plan) {
 //   producer set 0 (MT*4 warps)  K entries 0..31 of each A chunk into a TMEM ring
 //   producer set 1 (MT*4 warps)  K entries 32..63; then accumulators -> U, one
 //                                32-row quarter of one tile each
-//   MMA warp                     tcgen05.mma into accumulator buffer (unit % nacc)
+//   MMA warps (one per tile)     tcgen05.mma into accumulator buffer (unit % nacc)
 //   load warp                    units, tables and B chunks (bulk copies)
 // The A and B rings run on across unit boundaries, so set 0 and the load warp
 // stage the next unit's operands while set 1 drains the last one.
@@ -538,7 +538,7 @@ __global__ void __launch_bounds__(2 * 2 * TM + 96, 1) eval_gemm_kernel(qsft_plan
           }
           ce.next();
         }
-        // store and signal at once: the MMA warp waits for this chunk, not for the next one's compute
+        // store and signal at once: the MMA threads wait for this chunk, not for the next one's compute
         tmem_st16(a_lane + fa.slot * (uint32_t)(MT * A_COLS), av);
         tmem_st_wait();
         tc_fence_before();
@@ -556,7 +556,7 @@ __global__ void __launch_bounds__(2 * 2 * TM + 96, 1) eval_gemm_kernel(qsft_plan
       float2* __restrict__ ur = x.U + l;
       const float inv = *reinterpret_cast<const float*>(x.region);
       int ready = 1;
-      // one accumulator buffer: the MMA warp waits for this drain, so notice the
+      // one accumulator buffer: the MMA threads wait for this drain, so notice the
       // unit's end soon (128 ns cap); two: the drain overlaps MMAs, sleep longer
       if (lane == 0) ready = !*abort_flag && mbar_wait_sleep(&accf[ac.slot], ac.phase, nacc == 1 ? 128u : 2048u);
       ready = __shfl_sync(~0u, ready, 0);
@@ -833,8 +833,8 @@ extern "C" int qsft_gemm_layout(const qsft_job* jobs, int njobs, qsft_plan* plan
     npmax = npmax > g.NP ? npmax : g.NP;
   }
   // tensor memory: nacc accumulator buffers of mt tiles + at least two A slots.
-  // Preference: the larger mt (a B chunk feeds more rows, and the MMA warp's
-  // per-chunk waits and commit cover twice the MMAs), then at least three A
+  // Preference: the larger mt (a B chunk feeds more rows, and the per-chunk
+  // waits and commits cover twice the MMAs), then at least three A
   // slots, then two buffers (the epilogue overlaps the next unit's MMAs).
   // Presets cap mt and nacc.
   const int mt_cap = (plan->gm_mt == 1 || plan->gm_mt == 2) ? plan->gm_mt : 2;
