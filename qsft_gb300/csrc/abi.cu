@@ -10,12 +10,18 @@
 
 namespace qsft {
 
-// one block per job: compact the recorded balls (count > 0) into the output
-__global__ void collect_kernel(qsft_plan plan, uint8_t* out_k, double* out_val, int32_t* out_cnt,
-                               int64_t* out_index, unsigned long long* out_total) {
+// one block per job: compact the recorded balls (count > 0) into the output.
+// 1024 threads, positions taken a warp at a time (one shared atomic per warp)
+// and k rows copied 16 bytes at a time when the buffers and kstride allow
+constexpr int COLLECT_THREADS = 1024;
+__global__ void __launch_bounds__(COLLECT_THREADS) collect_kernel(qsft_plan plan, uint8_t* out_k, double* out_val,
+                                                                  int32_t* out_cnt, int64_t* out_index,
+                                                                  unsigned long long* out_total) {
   const int jid = blockIdx.x;
   const qsft_job* job = plan.jobs + jid;
   const int nb = min(plan.ctrl[jid].n_balls, job->ball_cap);
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
   __shared__ int count;
   __shared__ int pos;
   __shared__ unsigned long long start;
@@ -24,9 +30,11 @@ __global__ void collect_kernel(qsft_plan plan, uint8_t* out_k, double* out_val, 
     pos = 0;
   }
   __syncthreads();
-  int mine = 0;
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) mine += plan.ball_cnt[job->off_ball + i] > 0;
-  atomicAdd(&count, mine);
+  for (int i0 = 0; i0 < nb; i0 += blockDim.x) {  // uniform over the warp
+    const int i = i0 + threadIdx.x;
+    const unsigned m = __ballot_sync(~0u, i < nb && plan.ball_cnt[job->off_ball + i] > 0);
+    if (lane == 0 && m) atomicAdd(&count, __popc(m));
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     start = atomicAdd(out_total, (unsigned long long)count);
@@ -35,14 +43,26 @@ __global__ void collect_kernel(qsft_plan plan, uint8_t* out_k, double* out_val, 
   }
   __syncthreads();
   const int ks = plan.kstride;
-  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+  const bool vec = ((reinterpret_cast<uintptr_t>(out_k) | reinterpret_cast<uintptr_t>(plan.ball_k) | (uintptr_t)ks) & 15) == 0;
+  for (int i0 = 0; i0 < nb; i0 += blockDim.x) {
+    const int i = i0 + threadIdx.x;
     const int64_t src = job->off_ball + i;
-    const int c = plan.ball_cnt[src];
+    const int c = i < nb ? plan.ball_cnt[src] : 0;
+    const unsigned m = __ballot_sync(~0u, c > 0);
+    int base = 0;
+    if (lane == 0 && m) base = atomicAdd(&pos, __popc(m));
+    base = __shfl_sync(~0u, base, 0);
     if (c <= 0) continue;
-    const int64_t row = (int64_t)start + atomicAdd(&pos, 1);
-    const uint32_t* ks_src = reinterpret_cast<const uint32_t*>(plan.ball_k + src * ks);
-    uint32_t* ks_dst = reinterpret_cast<uint32_t*>(out_k + row * ks);
-    for (int w = 0; w < ks / 4; ++w) ks_dst[w] = ks_src[w];
+    const int64_t row = (int64_t)start + base + __popc(m & below);
+    if (vec) {
+      const uint4* ks_src = reinterpret_cast<const uint4*>(plan.ball_k + src * ks);
+      uint4* ks_dst = reinterpret_cast<uint4*>(out_k + row * ks);
+      for (int w = 0; w < ks / 16; ++w) ks_dst[w] = ks_src[w];
+    } else {
+      const uint32_t* ks_src = reinterpret_cast<const uint32_t*>(plan.ball_k + src * ks);
+      uint32_t* ks_dst = reinterpret_cast<uint32_t*>(out_k + row * ks);
+      for (int w = 0; w < ks / 4; ++w) ks_dst[w] = ks_src[w];
+    }
     out_val[2 * row] = plan.ball_sum[2 * src] / c;
     out_val[2 * row + 1] = plan.ball_sum[2 * src + 1] / c;
     out_cnt[row] = c;
@@ -174,7 +194,7 @@ extern "C" int qsft_collect(const qsft_plan* plan, uint8_t* out_k, double* out_v
       !out_val || !out_cnt || !out_index || !out_total)
     return QSFT_ERR_ARG;
   if (cudaMemsetAsync(out_total, 0, sizeof(int64_t), (cudaStream_t)stream) != cudaSuccess) return QSFT_ERR_CUDA;
-  collect_kernel<<<plan->njobs, 256, 0, (cudaStream_t)stream>>>(*plan, out_k, out_val, out_cnt, out_index,
+  collect_kernel<<<plan->njobs, COLLECT_THREADS, 0, (cudaStream_t)stream>>>(*plan, out_k, out_val, out_cnt, out_index,
                                                                    reinterpret_cast<unsigned long long*>(out_total));
   QSFT_CUDA_CHECK_LAUNCH();
   return QSFT_OK;
