@@ -424,12 +424,28 @@ class Batch:
             raise ValueError("specs do not match this batch's layout")
         self.specs = specs
         jobs = self.jobs_host
-        i8 = self.i8_host.numpy()
-        a = self.A_host.numpy()
+        self._pack_host(specs, self.i8_host.numpy(), self.A_host.numpy())
+        self.jobs_host_t.numpy()[:] = np.frombuffer(bytes(jobs), dtype=np.uint8)
+        st = stream if stream is not None else torch.cuda.current_stream(self.device)
+        with torch.cuda.stream(st):
+            self.i8.copy_(self.i8_host, non_blocking=True)
+            self.A.copy_(self.A_host, non_blocking=True)
+            self.jobs_dev.copy_(self.jobs_host_t, non_blocking=True)
+            for j, sp in enumerate(specs):
+                if sp.U is not None:
+                    n_el = sp.C * sp.R * sp.P * sp.B
+                    self.U[jobs[j].off_U:jobs[j].off_U + n_el].copy_(sp.U.reshape(-1).to(self.cdt))
+        self.h2d_bytes = self.i8.numel() + self.A.numel() * self.A.element_size() + self.jobs_dev.numel()
+
+    def _pack_host(self, specs, i8, a):
+        """The jobs' per-step fields into the host job records, and their M, D, K
+        digits and coefficients into the host arrays `i8` and `a` at the
+        layout's offsets (one concatenation per array: each job's M, D and K
+        rows followed by the zeros up to the next 16-byte boundary)."""
         pieces, apieces = [], []
         empty = np.zeros(0, np.int8)
         for j, sp in enumerate(specs):
-            jb = jobs[j]
+            jb = self.jobs_host[j]
             jb.max_iter = sp.max_iter
             jb.cutoff = sp.cutoff
             jb.noise_nu = sp.noise_nu
@@ -442,17 +458,6 @@ class Batch:
             np.concatenate(pieces, out=i8[:self.n_i8], casting="same_kind")
         if apieces:
             np.concatenate(apieces, out=a[:self.n_a], casting="same_kind")
-        self.jobs_host_t.numpy()[:] = np.frombuffer(bytes(jobs), dtype=np.uint8)
-        st = stream if stream is not None else torch.cuda.current_stream(self.device)
-        with torch.cuda.stream(st):
-            self.i8.copy_(self.i8_host, non_blocking=True)
-            self.A.copy_(self.A_host, non_blocking=True)
-            self.jobs_dev.copy_(self.jobs_host_t, non_blocking=True)
-            for j, sp in enumerate(specs):
-                if sp.U is not None:
-                    n_el = sp.C * sp.R * sp.P * sp.B
-                    self.U[jobs[j].off_U:jobs[j].off_U + n_el].copy_(sp.U.reshape(-1).to(self.cdt))
-        self.h2d_bytes = self.i8.numel() + self.A.numel() * self.A.element_size() + self.jobs_dev.numel()
 
     # ------------------------------------------------------------ steps
     def job_U(self, j):
