@@ -284,8 +284,13 @@ __device__ __forceinline__ void scan_phase(const qsft_plan& plan, int first) {
       if (__ldcg(&c->done)) return -1;
       return first ? plan.jobs[jid].C * plan.jobs[jid].B : __ldcg(&c->n_dirty[__ldcg(&c->iter) & 1]);
     });
+  // Jobs last to first: the pass before a scan (the transform, or the previous
+  // iteration's peel) walks them first to last, so the bins of the last jobs
+  // are the ones still in L2 when the scan starts (16 transforms: first scan
+  // 79.7 -> 71.5 us, second 70 -> 67 us against first-to-last)
   int64_t chunk0 = 0;  // 32-bin chunks of all jobs are dealt round-robin to the warps
-  for (int jid = 0; jid < plan.njobs; ++jid) {
+  for (int jj = 0; jj < plan.njobs; ++jj) {
+    const int jid = plan.njobs - 1 - jj;
     qsft_ctrl* ctl = plan.ctrl + jid;
     int cnt;
     if (win) {
