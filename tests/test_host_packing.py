@@ -4,10 +4,13 @@ exactly the per-job layout the workspace offsets describe, zero padding
 included; and the result parsing (one conversion for all rows, a view per
 job) gives every job's keys -- high parts of coded entries included --,
 values and counts, in arrays that do not share memory with the staging
-buffers the next read-back overwrites."""
+buffers the next read-back overwrites; a device error in the read-back (a
+job's table overflow in its control record, a nonzero status word) raises
+instead of returning truncated results."""
 import ctypes
 
 import numpy as np
+import pytest
 import torch
 
 from qsft_gb300 import _lib
@@ -55,13 +58,13 @@ def test_pack_host_matches_layout():
     assert np.array_equal(a[:b.n_a], wa[:b.n_a])
 
 
-def test_parse_views_and_coded_keys():
-    specs = _specs()
-    b = _host_batch(specs)
+def _read_back(b, counts, seed=11):
+    """Synthetic read-back buffers of a batch: metadata (row count, per-job
+    output index with the jobs' rows in reverse order, control records, status
+    word) and random output rows."""
     J, ks = b.njobs, b.kstride
     cs = ctypes.sizeof(_lib.QsftCtrl) // 8
-    rng = np.random.RandomState(11)
-    counts = [5, 0, 7, 3]
+    rng = np.random.RandomState(seed)
     total = sum(counts)
     meta = np.zeros(1 + 2 * J + cs * J + 1, np.int64)
     meta[0] = total
@@ -73,6 +76,14 @@ def test_parse_views_and_coded_keys():
     out_val = rng.randn((total + 4) * 2)
     out_cnt = rng.randint(1, 5, size=total + 4).astype(np.int32)
     b.meta = torch.zeros(meta.size, dtype=torch.int64)
+    return meta, out_k, out_val, out_cnt
+
+
+def test_parse_views_and_coded_keys():
+    specs = _specs()
+    b = _host_batch(specs)
+    ks = b.kstride
+    meta, out_k, out_val, out_cnt = _read_back(b, [5, 0, 7, 3])
     res = b._parse(meta, out_k, out_val, out_cnt)
     rows_k = out_k.reshape(-1, ks)
     for j, (keys, vals, cnts, ctrl) in enumerate(res):
@@ -91,3 +102,20 @@ def test_parse_views_and_coded_keys():
     out_cnt[:] = 0
     for (k, v, c, _), (k0, v0, c0) in zip(res, saved):
         assert np.array_equal(k, k0) and np.array_equal(v, v0) and np.array_equal(c, c0)
+
+
+def test_parse_raises_on_device_errors():
+    b = _host_batch(_specs())
+    J = b.njobs
+    meta, out_k, out_val, out_cnt = _read_back(b, [5, 0, 7, 3])
+    # job 2's ball table overflowed: its control record's err field
+    raw = meta.view(np.uint8)
+    at = (1 + 2 * J) * 8 + 2 * ctypes.sizeof(_lib.QsftCtrl) + _lib.QsftCtrl.err.offset
+    raw[at:at + 4] = np.frombuffer(np.int32(-4).tobytes(), np.uint8)      # QSFT_ERR_OVERFLOW
+    with pytest.raises(_lib.QsftError, match="job 2"):
+        b._parse(meta, out_k, out_val, out_cnt)
+    # a bounded device wait gave up: the status word (low 32 bits of the last word)
+    meta, out_k, out_val, out_cnt = _read_back(b, [5, 0, 7, 3])
+    meta[-1] = np.int64(np.uint32(np.int32(-5)))                             # QSFT_ERR_TIMEOUT
+    with pytest.raises(_lib.QsftError, match="device status -5"):
+        b._parse(meta, out_k, out_val, out_cnt)
